@@ -1,0 +1,332 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 k-core peel (one JSON line on rank 0).
+
+Default workload: the single-graph R-MAT scale-20 edge-factor-5 peel (1,048,576
+vertices, 5,242,880 directed draws, a/b/c/d = .57/.19/.19/.05, seed 2),
+symmetrised and deduplicated, uint32 CSR resident in HBM.  A step is one full
+peel of that graph (every level until all vertices are peeled).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|2|3] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU restatement (the
+level-synchronous peel of src/ours.cc:117-160, oracle/kc_oracle.c) on all host
+cores; the reference has no CPU peel of its own.  Multi-GPU runs are replicas
+(one independent graph per rank, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import platform
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "k-core edges/s & HBM GB/s; batched graphs/s, p50/p99 latency vs plain peel"
+L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
+
+# DRAM bytes per launch of the persistent peel kernel from one ncu capture of
+# the same workload (profiles/peel_persistent_*.md); None until captured.
+NCU_TRAFFIC = {}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.p is None:
+            return
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 7:
+                self.rows.append(f)
+
+    def summary(self) -> dict:
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if "Active" in r[3 + i]
+                          and "Not" not in r[3 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def cpu_model() -> str:
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
+def reference_arm(args, rank, world):
+    """The reference algorithm on the host cores (CPU restatement, all threads)."""
+    if rank != 0:
+        return
+    from kcoregpu_gb300 import workloads as W
+    from oracle import kc_oracle as O
+    off, nbr = W.single_graph(args.config)
+    m = len(nbr) // 2
+    nth = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        O.levelsync(off, nbr, nthreads=nth)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, kmax, levels = O.levelsync(off, nbr, nthreads=nth)
+        times.append(time.perf_counter() - t0)
+    t = sum(times) / len(times)
+    val = m / t
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "edges/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": W.SINGLE[args.config]["name"], "V": len(off) - 1, "undirected_edges": m,
+                   "kmax": kmax, "levels": levels},
+        "cpu_baseline": {"value": val, "unit": "edges/s", "cores": nth, "kind": "port",
+                         "sample": f"full graph x {args.steps} peels (level-synchronous restatement of "
+                                   f"src/ours.cc:117-160, OpenMP, {cpu_model()})"},
+        "e2e": {"value": val, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def cpu_baseline(off, nbr):
+    """The project's single-thread BZ bucket peel timed on the same CSR."""
+    from oracle import kc_oracle as O
+    m = len(nbr) // 2
+    reps, t_tot = 0, 0.0
+    while t_tot < 3.0 and reps < 50:
+        t0 = time.perf_counter()
+        O.bz(off, nbr)
+        t_tot += time.perf_counter() - t0
+        reps += 1
+    return {"value": m * reps / t_tot, "unit": "edges/s", "cores": 1, "kind": "port",
+            "sample": f"full graph x {reps} Batagelj-Zaversnik peels, single thread ({cpu_model()}, "
+                      f"{os.cpu_count()} cores on host)"}
+
+
+def reference_gpu(off, nbr, tmpdir: Path):
+    """The reference's own GPU kernels (src/ours.cc, unmodified cubin) with its
+    host loop replayed; None when the prebuilt cubin is absent."""
+    cubin = ROOT / "oracle" / "_ref" / "ref_peel.cubin"
+    drv = ROOT / "oracle" / "_build" / "ref_peel_driver"
+    if not cubin.exists() or not drv.exists():
+        return None
+    tmpdir.mkdir(parents=True, exist_ok=True)
+    f = tmpdir / "csr.bin"
+    with open(f, "wb") as fh:
+        np.array([len(off) - 1, len(nbr)], np.uint32).tofile(fh)
+        off.tofile(fh)
+        nbr.tofile(fh)
+    out = tmpdir / "core.bin"
+    r = subprocess.run([str(drv), str(cubin), str(f), str(out)], capture_output=True, text=True,
+                       timeout=300)
+    if r.returncode != 0:
+        return {"unavailable": (r.stderr or r.stdout).strip()[:200]}
+    tok = r.stdout.split()
+    ms = float(tok[tok.index("ms") + 1])
+    return {"ms": ms, "edges_per_s": (len(nbr) // 2) / (ms / 1e3),
+            "kmax": int(tok[tok.index("kmax") + 1]),
+            "core": np.fromfile(out, dtype=np.uint32)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return reference_arm(args, rank, world)
+
+    import torch
+    import kcoregpu_gb300 as kc
+    from kcoregpu_gb300 import workloads as W
+    from oracle import kc_oracle as O
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    off, nbr = W.single_graph(args.config)
+    V, arcs = len(off) - 1, len(nbr)
+    m = arcs // 2
+    stream = torch.cuda.Stream()
+    g = kc.DeviceGraph(off, nbr)
+    g.set_stream(stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+
+    # correctness of the benchmarked graph (untimed)
+    core, kmax, st0 = g.peel()
+    want, wk = O.bz(off, nbr)
+    if not (np.array_equal(core, want) and kmax == wk):
+        raise SystemExit("bench: GPU core numbers differ from the oracle")
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            g.peel_async()
+        stream.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        kern_ms = []
+        barrier()
+        torch.cuda.synchronize()
+        with Clocks(local) as clk:
+            t_wall = time.perf_counter()
+            for i in range(args.steps):
+                flush.zero_()                   # L2 flushed between timed steps
+                starts[i].record(stream)
+                g.peel_async()
+                ends[i].record(stream)
+                _, _, st = g.fetch(want_core=False)   # kernel-only time from the library's events
+                kern_ms.append(st["peel_ms"])
+            torch.cuda.synchronize()
+            t_wall = time.perf_counter() - t_wall
+        barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    kms = sum(kern_ms) / len(kern_ms)
+    if world > 1:
+        t = torch.tensor([ms, kms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms, kms = t.tolist()
+
+    # end to end through the public one-shot call: pinned H2D of the CSR, the
+    # peel, D2H of the core numbers, every step
+    lib = kc.lib()
+    h_off = lib.kc_host_alloc(4 * (V + 1))
+    h_nbr = lib.kc_host_alloc(4 * max(arcs, 1))
+    h_core = lib.kc_host_alloc(4 * max(V, 1))
+    a_off = np.ctypeslib.as_array(C.cast(h_off, C.POINTER(C.c_uint32)), shape=(V + 1,))
+    a_nbr = np.ctypeslib.as_array(C.cast(h_nbr, C.POINTER(C.c_uint32)), shape=(max(arcs, 1),))
+    a_off[:] = off
+    a_nbr[:arcs] = nbr
+    u32p = C.POINTER(C.c_uint32)
+    kout = C.c_uint32()
+
+    def e2e_call():
+        rc = lib.kc_peel_csr(C.cast(h_off, u32p), C.cast(h_nbr, u32p), V, C.cast(h_core, u32p), C.byref(kout))
+        if rc:
+            raise SystemExit(f"kc_peel_csr failed: {rc}")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_call()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_call()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / len(e2e_t)
+    got = np.ctypeslib.as_array(C.cast(h_core, u32p), shape=(V,))
+    if not np.array_equal(got, want):
+        raise SystemExit("bench: e2e core numbers differ from the oracle")
+    for p in (h_off, h_nbr, h_core):
+        lib.kc_host_free(p)
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak_hbm()
+    B = W.algorithmic_bytes(V, arcs, kmax)
+    achieved = B / (kms / 1e3) / 1e9
+    value = world * m / (ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": W.SINGLE[args.config]["name"], "V": V, "undirected_edges": m, "arcs": arcs,
+                   "kmax": kmax, "levels": kmax + 1, "parallelism": f"replicas{world}",
+                   "l2": "flushed between timed steps (512 MiB write)", "inputs": "resident in HBM"},
+        "hbm_gbs": achieved, "arcs_per_s": world * arcs / (ms / 1e3),
+        "kernel_ms": kms,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind + " hbm_gbs",
+                     "algorithmic_bytes": B,
+                     "traffic": NCU_TRAFFIC.get(args.config)},
+        "e2e": {"value": world * m / e2e_s, "unit": "edges/s", "ms": e2e_s * 1e3,
+                "h2d_bytes_per_step": 4 * (V + 1) + 4 * arcs, "d2h_bytes_per_step": 4 * V},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "wall_s": t_wall,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(off, nbr)
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        ref = reference_gpu(off, nbr, Path(td))
+        if ref is not None and "core" in ref:
+            ref["bit_exact_vs_oracle"] = bool(np.array_equal(ref.pop("core"), want))
+    if ref is not None:
+        line["reference_gpu"] = ref
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/*
+ * kcore.h - C ABI of the GB300 k-core peel (libkcore_gb300.so).
+ *
+ * Drop-in boundary for the reference's single hot path, the level-synchronous
+ * peel behind `kcore <edgelist>`.  Every entry point returns 0 (KC_OK) or a
+ * negative KC_ERR_* code; none calls exit().  Host buffers are owned by the
+ * caller unless a function says otherwise.  Reference citations are paths
+ * inside akhlaqueak/KCoreGPU.
+ *
+ * Threading: a kc_graph / kc_batch is used by one host thread at a time.
+ * kc_serve_submit / kc_serve_poll may be called from any thread.
+ */
+#ifndef KCORE_GB300_H
+#define KCORE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (replace chkerr()'s exit(-1), inc/gpu_memory_allocation.h:9-16,
+ *      and the device assert() on queue overflow, src/buffer.cc:2) ---- */
+#define KC_OK            0
+#define KC_ERR_IO       -1   /* file cannot be opened / written                    */
+#define KC_ERR_PARSE    -2   /* malformed edge list or serialized cache            */
+#define KC_ERR_OOM      -3   /* host or device allocation failed                   */
+#define KC_ERR_OVERFLOW -4   /* a device queue would overflow (no trap)            */
+#define KC_ERR_TIMEOUT  -5   /* a bounded device wait gave up                      */
+#define KC_ERR_CUDA     -6   /* CUDA runtime error                                 */
+#define KC_ERR_BUDGET   -7   /* request exceeds the server's HBM budget            */
+#define KC_ERR_INVALID  -8   /* bad argument (null pointer, size limit)            */
+#define KC_ERR_NODEV    -9   /* no CUDA device                                     */
+#define KC_ERR_BUSY    -10   /* server queue full / result not ready               */
+#define KC_ERR_CLOSED  -11   /* server already closed                              */
+
+const char* kc_strerror(int code);
+/* Message of the last failure on the calling thread (empty when none).          */
+const char* kc_last_error(void);
+/* SM count, persistent grid size and compute capability of the current device. */
+int  kc_device_info(int* sms, int* grid, int* cc_major, int* cc_minor);
+/* Page-locked host buffers for the H2D/D2H staging of the calls below.         */
+void* kc_host_alloc(size_t bytes);
+void  kc_host_free(void* p);
+
+/* ---- host CSR (the reference's Graph arrays, inc/graph.h:7-23) ---- */
+typedef struct kc_csr_host {
+    uint32_t  V;          /* vertices: max id + 1 (graph.cpp:90-96)              */
+    uint32_t  E;          /* arcs = offsets[V] = 2 x undirected edges (graph.cpp:114) */
+    uint32_t* offsets;    /* V+1 exclusive prefix of degrees (graph.cpp:110-113)  */
+    uint32_t* neighbors;  /* E, ascending within each vertex (graph.cpp:117-122)  */
+    uint32_t* degrees;    /* V (graph.cpp:105-108)                                */
+} kc_csr_host;
+
+/* Parse modes for the SNAP-style text loader.                                   */
+#define KC_PARSE_SNAP       0  /* default: skip lines starting with a letter (graph.cpp:86)
+                                  and also '#', '%' and blank lines                 */
+#define KC_PARSE_REFERENCE  1  /* byte-for-byte reference stream semantics: a '#'/'%'
+                                  line yields s=0 and keeps the previous t
+                                  (graph.cpp:86-88); a first line without a
+                                  previous t is KC_ERR_PARSE (undefined there)       */
+
+/* Graph::readFile (graph.cpp:58-124): text edge list -> deduplicated, symmetrised
+ * CSR with self-loops dropped; V = max id + 1.  Arrays are malloc'ed; free them
+ * with kc_csr_free.  Parallel radix CSR build, bytes identical to the reference. */
+int  kc_load_edgelist(const char* path, int parse_mode, kc_csr_host* out);
+
+/* Same CSR semantics from an in-memory directed edge array (src[i] -> dst[i]).  */
+int  kc_build_csr(const uint32_t* src, const uint32_t* dst, uint64_t n_edges,
+                  kc_csr_host* out);
+
+void kc_csr_free(kc_csr_host* csr);
+
+/* Graph::readSerialized / writeSerialized (graph.cpp:9-54): the text CSR cache
+ * "V\nE\n" deg[i]"\n"... off[i]" "... nbr[j]" "..., no trailing newline.         */
+int  kc_read_serialized(const char* path, kc_csr_host* out);
+int  kc_write_serialized(const char* path, const kc_csr_host* csr);
+
+/* Graph::Graph(path) (graph.cpp:142-154): read <cache_dir>/serialized-<basename>
+ * when present, else parse the text and write that cache (silently skipped when
+ * cache_dir is missing).  cache_dir NULL means "./output/" (inc/common.h:17).
+ * *from_cache is set to 1 when the cache was used (may be NULL).                */
+int  kc_load_graph(const char* path, const char* cache_dir, int parse_mode,
+                   kc_csr_host* out, int* from_cache);
+
+/* Graph::writeKCoreToDisk (graph.cpp:126-140): JSON '{ "v": c, \n... }\n',
+ * vertices with core 0 omitted.                                                 */
+int  kc_write_core_json(const char* path, const uint32_t* core, uint32_t V);
+/* The verification notebook's "id core" text format, one line per vertex
+ * (.ipynb_checkpoints/test-checkpoint.ipynb cell 4).                            */
+int  kc_write_core_txt(const char* path, const uint32_t* core, uint32_t V);
+
+/* ---- synthetic graph generators (seeded, deterministic on any host) ---- */
+/* R-MAT: n vertices (scale = ceil(log2 n), endpoints >= n redrawn), n_edges
+ * directed draws, probabilities a,b,c (d = 1-a-b-c), then a seeded relabel.     */
+int  kc_gen_rmat(uint32_t n, uint64_t n_edges, double a, double b, double c,
+                 uint64_t seed, uint32_t* src, uint32_t* dst);
+/* Chung-Lu power law: weights w_i ~ (i+i0)^(-1/(gamma-1)) scaled to max_w and
+ * sum 2*m_target, endpoints by alias sampling, deduplicated and topped up to
+ * m_target undirected edges, seeded relabel.  Writes m_target pairs.           */
+int  kc_gen_chung_lu(uint32_t n, uint64_t m_target, double gamma, double max_w,
+                     uint64_t seed, uint32_t* src, uint32_t* dst);
+/* Erdos-Renyi G(n, m): m distinct undirected pairs, no self-loops.              */
+int  kc_gen_er(uint32_t n, uint64_t m, uint64_t seed, uint32_t* src, uint32_t* dst);
+/* Writes "u\tv\n" lines (no comment or blank lines).                            */
+int  kc_write_edgelist(const char* path, const uint32_t* src, const uint32_t* dst,
+                       uint64_t n_edges);
+
+/* ---- single-graph peel (replaces kcore(), src/ours.cc:117-160) ---- */
+typedef struct kc_stats {
+    uint32_t V;
+    uint32_t kmax;         /* degeneracy = level-1 at loop exit (ours.cc:151)    */
+    uint32_t levels;       /* level iterations run = kmax+1                      */
+    uint32_t blocks;       /* persistent CTAs launched                           */
+    uint64_t arcs;         /* offsets[V]                                         */
+    uint64_t tasks;        /* hub chunks / spilled vertices pushed to the queue  */
+    float    peel_ms;      /* device time of the peel (CUDA events)              */
+    float    total_ms;     /* host wall time of the call                         */
+} kc_stats;
+
+typedef struct kc_graph kc_graph;   /* device-resident CSR + peel state         */
+
+/* Pinned H2D upload of a CSR (malloc_graph_gpu_memory, gpu_memory_allocation.cu:4-12).
+ * degrees are derived on the device from offsets.                              */
+int  kc_graph_upload(const uint32_t* offsets, const uint32_t* neighbors, uint32_t V,
+                     kc_graph** g);
+/* Use an existing CUDA stream (cudaStream_t passed as void*; NULL = own stream). */
+int  kc_graph_set_stream(kc_graph* g, void* stream);
+/* Runs the peel on the device (no host sync).  Results stay on the device.      */
+int  kc_graph_peel_async(kc_graph* g);
+/* Waits for the last peel, copies core numbers (V uint32, may be NULL) and
+ * kmax to the host (get_results_from_gpu, gpu_memory_allocation.cu:14-16).       */
+int  kc_graph_fetch(kc_graph* g, uint32_t* core_out, uint32_t* kmax, kc_stats* st);
+/* kc_graph_peel_async + kc_graph_fetch.                                          */
+int  kc_peel(kc_graph* g, uint32_t* core_out, uint32_t* kmax, kc_stats* st);
+/* Peel order (vertices by level; the kcore-global-buffer glBuffer, KCore.h:80)
+ * and k-shell offsets (cShellOffsets, KCore.h:266): order_out[V],
+ * shell_offsets_out[kmax+2].  Runs a peel that records the order.                */
+int  kc_degeneracy_order(kc_graph* g, uint32_t* order_out,
+                         uint32_t* shell_offsets_out, uint32_t shell_cap,
+                         uint32_t* kmax);
+/* Device pointers of the resident CSR/core arrays (for zero-copy consumers).     */
+int  kc_graph_device_ptrs(kc_graph* g, const uint32_t** d_offsets,
+                          const uint32_t** d_neighbors, uint32_t** d_core);
+void kc_graph_free(kc_graph* g);
+
+/* One-shot: host CSR in, host core numbers out (pinned staging, cached device
+ * buffers per device).  kmax as the reference computes it (0xFFFFFFFF for V=0). */
+int  kc_peel_csr(const uint32_t* offsets, const uint32_t* neighbors, uint32_t V,
+                 uint32_t* core_out, uint32_t* kmax);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KCORE_GB300_H */

@@ -1,0 +1,410 @@
+// C ABI of the single-graph peel: device-resident graphs (kc_graph), the
+// persistent cooperative launch, and the one-shot host-buffer entry point.
+// Replaces the reference's kcore() host loop (src/ours.cc:117-160) and its
+// device memory glue (src/gpu_memory_allocation.cu:4-22).
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kc_internal.h"
+#include "kc_peel.cuh"
+
+using kc::PeelArgs;
+using kc::PeelCtl;
+
+namespace kc {
+
+int cuda_fail(cudaError_t e, const char* what) {
+    set_error_msg(std::string(what) + ": " + cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) return KC_ERR_OOM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return KC_ERR_NODEV;
+    return KC_ERR_CUDA;
+}
+
+#define KC_CUDA(call)                                       \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+// Persistent grid size per device: SMs x co-resident CTAs.
+static int persistent_grid(int dev) {
+    static std::mutex mu;
+    static std::vector<int> cache;
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+    if (cache[dev]) return cache[dev];
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_persistent_fn(), kPeelThreads, 0);
+    if (per < 1) per = 1;
+    cache[dev] = sms * per;
+    return cache[dev];
+}
+
+}  // namespace kc
+
+using namespace kc;
+
+struct kc_graph {
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint32_t V = 0;
+    uint64_t E = 0;
+    uint32_t maxdeg = 0;
+    uint32_t cap_V = 0;      // allocated vertex capacity
+    uint64_t cap_E = 0;      // allocated arc capacity
+    uint32_t* d_off = nullptr;
+    uint32_t* d_nbr = nullptr;
+    uint32_t* d_w = nullptr;
+    uint32_t* d_core = nullptr;
+    uint32_t* d_order = nullptr;
+    uint32_t* d_shells = nullptr;
+    unsigned long long* d_tasks = nullptr;
+    unsigned long long task_cap = 0;
+    PeelCtl* d_ctl = nullptr;
+    PeelCtl* h_ctl = nullptr;   // pinned
+    uint32_t epoch = 0;
+    int grid = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool pending = false;
+    bool ran = false;
+    bool with_order = false;
+    uint32_t shell_cap = 0;
+};
+
+namespace {
+
+void release(kc_graph* g) {
+    if (!g) return;
+    cudaSetDevice(g->dev);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    cudaFree(g->d_off); cudaFree(g->d_nbr); cudaFree(g->d_w); cudaFree(g->d_core);
+    cudaFree(g->d_order); cudaFree(g->d_shells); cudaFree(g->d_tasks); cudaFree(g->d_ctl);
+    if (g->h_ctl) cudaFreeHost(g->h_ctl);
+    if (g->ev0) cudaEventDestroy(g->ev0);
+    if (g->ev1) cudaEventDestroy(g->ev1);
+    if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+}
+
+uint64_t task_capacity(uint32_t V, uint64_t E) { return (uint64_t)V + E / kChunk + 64; }
+
+// (Re)allocates device buffers for a graph of V vertices / E arcs.
+int reserve(kc_graph* g, uint32_t V, uint64_t E) {
+    const uint32_t Vpad = (V + 127u) / 128u * 128u;
+    if (V > g->cap_V || !g->d_off) {
+        cudaFree(g->d_off); cudaFree(g->d_w); cudaFree(g->d_core); cudaFree(g->d_order);
+        cudaFree(g->d_shells);
+        g->d_off = g->d_w = g->d_core = g->d_order = g->d_shells = nullptr;
+        KC_CUDA(cudaMalloc(&g->d_off, sizeof(uint32_t) * ((size_t)Vpad + 4)));
+        KC_CUDA(cudaMalloc(&g->d_w, sizeof(uint32_t) * ((size_t)Vpad + 4)));
+        KC_CUDA(cudaMalloc(&g->d_core, sizeof(uint32_t) * ((size_t)Vpad + 4)));
+        g->cap_V = V;
+    }
+    if (E > g->cap_E || !g->d_nbr) {
+        cudaFree(g->d_nbr);
+        g->d_nbr = nullptr;
+        KC_CUDA(cudaMalloc(&g->d_nbr, sizeof(uint32_t) * (E ? E : 1)));
+        g->cap_E = E;
+    }
+    const unsigned long long tc = task_capacity(g->cap_V, g->cap_E);
+    if (tc > g->task_cap || !g->d_tasks) {
+        cudaFree(g->d_tasks);
+        g->d_tasks = nullptr;
+        KC_CUDA(cudaMalloc(&g->d_tasks, sizeof(unsigned long long) * tc));
+        KC_CUDA(cudaMemsetAsync(g->d_tasks, 0, sizeof(unsigned long long) * tc, g->stream));
+        g->task_cap = tc;
+        g->epoch = 0;
+    }
+    return KC_OK;
+}
+
+int graph_create(kc_graph** out) {
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        set_error_msg("no CUDA device is available");
+        return KC_ERR_NODEV;
+    }
+    kc_graph* g = new kc_graph();
+    KC_CUDA(cudaGetDevice(&g->dev));
+    KC_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+    g->own_stream = true;
+    KC_CUDA(cudaEventCreate(&g->ev0));
+    KC_CUDA(cudaEventCreate(&g->ev1));
+    KC_CUDA(cudaMalloc(&g->d_ctl, sizeof(PeelCtl)));
+    KC_CUDA(cudaMallocHost(&g->h_ctl, sizeof(PeelCtl)));
+    std::memset(g->h_ctl, 0, sizeof(PeelCtl));
+    g->grid = persistent_grid(g->dev);
+    *out = g;
+    return KC_OK;
+}
+
+int graph_load(kc_graph* g, const uint32_t* off, const uint32_t* nbr, uint32_t V) {
+    const uint64_t E = V ? off[V] : 0;
+    if (V && off[0] != 0) { set_error_msg("offsets[0] must be 0"); return KC_ERR_INVALID; }
+    uint32_t maxdeg = 0;
+    for (uint32_t v = 0; v < V; ++v) {
+        if (off[v + 1] < off[v]) { set_error_msg("offsets must be non-decreasing"); return KC_ERR_INVALID; }
+        maxdeg = std::max(maxdeg, off[v + 1] - off[v]);
+    }
+    if (maxdeg >= kBias) { set_error_msg("a degree above 2^30 is not supported"); return KC_ERR_INVALID; }
+    // Every neighbour id must name a vertex: the kernels index the state array
+    // with it.
+    uint32_t bad = 0;
+#pragma omp parallel for reduction(| : bad) schedule(static)
+    for (int64_t j = 0; j < (int64_t)E; ++j) bad |= (nbr[j] >= V);
+    if (bad) { set_error_msg("a neighbour id is >= V"); return KC_ERR_INVALID; }
+    int rc = reserve(g, V, E);
+    if (rc) return rc;
+    g->V = V;
+    g->E = E;
+    g->maxdeg = maxdeg;
+    if (V) KC_CUDA(cudaMemcpyAsync(g->d_off, off, sizeof(uint32_t) * ((size_t)V + 1), cudaMemcpyHostToDevice, g->stream));
+    if (E) KC_CUDA(cudaMemcpyAsync(g->d_nbr, nbr, sizeof(uint32_t) * E, cudaMemcpyHostToDevice, g->stream));
+    g->ran = false;
+    return KC_OK;
+}
+
+int graph_launch(kc_graph* g, bool with_order) {
+    KC_CUDA(cudaSetDevice(g->dev));
+    g->with_order = with_order;
+    if (g->V == 0) {   // the reference loop never runs: kmax = level-1 = 0xFFFFFFFF
+        std::memset(g->h_ctl, 0, sizeof(PeelCtl));
+        g->h_ctl->kmax = 0xFFFFFFFFu;
+        g->h_ctl->levels = 0;
+        g->pending = false;
+        g->ran = true;
+        KC_CUDA(cudaEventRecord(g->ev0, g->stream));
+        KC_CUDA(cudaEventRecord(g->ev1, g->stream));
+        return KC_OK;
+    }
+    if (with_order) {
+        const uint32_t sc = g->maxdeg + 2;
+        if (!g->d_order || sc > g->shell_cap) {
+            cudaFree(g->d_order); cudaFree(g->d_shells);
+            g->d_order = g->d_shells = nullptr;
+            KC_CUDA(cudaMalloc(&g->d_order, sizeof(uint32_t) * ((size_t)g->cap_V + 4)));
+            KC_CUDA(cudaMalloc(&g->d_shells, sizeof(uint32_t) * sc));
+            g->shell_cap = sc;
+        }
+    }
+    g->epoch = g->epoch % 255u + 1u;
+    if (g->epoch == 1u)
+        KC_CUDA(cudaMemsetAsync(g->d_tasks, 0, sizeof(unsigned long long) * g->task_cap, g->stream));
+    KC_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(PeelCtl), g->stream));
+    PeelArgs a;
+    a.off = g->d_off;
+    a.nbr = g->d_nbr;
+    a.w = g->d_w;
+    a.core = g->d_core;
+    a.order = with_order ? g->d_order : nullptr;
+    a.shells = with_order ? g->d_shells : nullptr;
+    a.tasks = g->d_tasks;
+    a.ctl = g->d_ctl;
+    a.task_cap = g->task_cap;
+    a.V = g->V;
+    a.shell_cap = with_order ? g->shell_cap : 0;
+    a.max_level = g->maxdeg;
+    a.epoch = g->epoch;
+    a.spin_limit = 1u << 22;
+    void* args[] = {&a};
+    KC_CUDA(cudaEventRecord(g->ev0, g->stream));
+    KC_CUDA(cudaLaunchCooperativeKernel(peel_persistent_fn(), dim3(g->grid), dim3(kPeelThreads), args, 0, g->stream));
+    KC_CUDA(cudaEventRecord(g->ev1, g->stream));
+    KC_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(PeelCtl), cudaMemcpyDeviceToHost, g->stream));
+    g->pending = true;
+    g->ran = true;
+    return KC_OK;
+}
+
+int graph_finish(kc_graph* g, kc_stats* st) {
+    KC_CUDA(cudaSetDevice(g->dev));
+    if (!g->ran) { set_error_msg("no peel has been run on this graph"); return KC_ERR_INVALID; }
+    KC_CUDA(cudaStreamSynchronize(g->stream));
+    g->pending = false;
+    if (g->h_ctl->err) {
+        set_error_msg(std::string("device peel failed at level ") + std::to_string(g->h_ctl->err_level));
+        return g->h_ctl->err;
+    }
+    if (st) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, g->ev0, g->ev1);
+        st->V = g->V;
+        st->kmax = g->h_ctl->kmax;
+        st->levels = g->h_ctl->levels;
+        st->blocks = (uint32_t)g->grid;
+        st->arcs = g->E;
+        st->tasks = g->h_ctl->tasks;
+        st->peel_ms = ms;
+    }
+    return KC_OK;
+}
+
+std::mutex g_oneshot_mu;
+std::vector<kc_graph*> g_oneshot;   // per device
+
+}  // namespace
+
+extern "C" {
+
+const char* kc_strerror(int code) {
+    switch (code) {
+        case KC_OK: return "ok";
+        case KC_ERR_IO: return "i/o error";
+        case KC_ERR_PARSE: return "parse error";
+        case KC_ERR_OOM: return "out of memory";
+        case KC_ERR_OVERFLOW: return "queue or size overflow";
+        case KC_ERR_TIMEOUT: return "bounded device wait timed out";
+        case KC_ERR_CUDA: return "CUDA error";
+        case KC_ERR_BUDGET: return "request exceeds the HBM budget";
+        case KC_ERR_INVALID: return "invalid argument";
+        case KC_ERR_NODEV: return "no CUDA device";
+        case KC_ERR_BUSY: return "busy / not ready";
+        case KC_ERR_CLOSED: return "closed";
+        default: return "unknown error";
+    }
+}
+
+int kc_graph_upload(const uint32_t* off, const uint32_t* nbr, uint32_t V, kc_graph** out) {
+    if (!out || (V && (!off || (off[V] && !nbr)))) { set_error_msg("null argument"); return KC_ERR_INVALID; }
+    *out = nullptr;
+    kc_graph* g = nullptr;
+    int rc = graph_create(&g);
+    if (rc) { if (g) { release(g); delete g; } return rc; }
+    rc = graph_load(g, off, nbr, V);
+    if (rc == KC_OK) {
+        cudaError_t e = cudaStreamSynchronize(g->stream);
+        if (e != cudaSuccess) rc = cuda_fail(e, "upload");
+    }
+    if (rc) { release(g); delete g; return rc; }
+    *out = g;
+    return KC_OK;
+}
+
+int kc_graph_set_stream(kc_graph* g, void* stream) {
+    if (!g) return KC_ERR_INVALID;
+    cudaSetDevice(g->dev);
+    if (g->stream) cudaStreamSynchronize(g->stream);
+    if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
+    if (stream) {
+        g->stream = (cudaStream_t)stream;
+        g->own_stream = false;
+    } else {
+        KC_CUDA(cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking));
+        g->own_stream = true;
+    }
+    return KC_OK;
+}
+
+int kc_graph_peel_async(kc_graph* g) {
+    if (!g) return KC_ERR_INVALID;
+    return graph_launch(g, false);
+}
+
+int kc_graph_fetch(kc_graph* g, uint32_t* core_out, uint32_t* kmax, kc_stats* st) {
+    if (!g) return KC_ERR_INVALID;
+    int rc = graph_finish(g, st);
+    if (rc) return rc;
+    if (core_out && g->V)
+        KC_CUDA(cudaMemcpy(core_out, g->d_core, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost));
+    if (kmax) *kmax = g->h_ctl->kmax;
+    return KC_OK;
+}
+
+int kc_peel(kc_graph* g, uint32_t* core_out, uint32_t* kmax, kc_stats* st) {
+    if (!g) return KC_ERR_INVALID;
+    auto t0 = std::chrono::steady_clock::now();
+    int rc = graph_launch(g, false);
+    if (rc) return rc;
+    rc = kc_graph_fetch(g, core_out, kmax, st);
+    if (st) st->total_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int kc_degeneracy_order(kc_graph* g, uint32_t* order_out, uint32_t* shells_out, uint32_t shell_cap,
+                        uint32_t* kmax) {
+    if (!g) return KC_ERR_INVALID;
+    int rc = graph_launch(g, true);
+    if (rc) return rc;
+    rc = graph_finish(g, nullptr);
+    if (rc) return rc;
+    const uint32_t km = g->h_ctl->kmax;
+    if (kmax) *kmax = km;
+    if (g->V == 0) {
+        if (shells_out && shell_cap) shells_out[0] = 0;
+        return KC_OK;
+    }
+    if (order_out) KC_CUDA(cudaMemcpy(order_out, g->d_order, sizeof(uint32_t) * g->V, cudaMemcpyDeviceToHost));
+    if (shells_out) {
+        const uint32_t need = km + 2;
+        if (shell_cap < need) { set_error_msg("shell_offsets_out needs kmax+2 entries"); return KC_ERR_INVALID; }
+        KC_CUDA(cudaMemcpy(shells_out, g->d_shells, sizeof(uint32_t) * need, cudaMemcpyDeviceToHost));
+    }
+    return KC_OK;
+}
+
+int kc_graph_device_ptrs(kc_graph* g, const uint32_t** d_off, const uint32_t** d_nbr, uint32_t** d_core) {
+    if (!g) return KC_ERR_INVALID;
+    if (d_off) *d_off = g->d_off;
+    if (d_nbr) *d_nbr = g->d_nbr;
+    if (d_core) *d_core = g->d_core;
+    return KC_OK;
+}
+
+void kc_graph_free(kc_graph* g) {
+    if (!g) return;
+    release(g);
+    delete g;
+}
+
+int kc_peel_csr(const uint32_t* off, const uint32_t* nbr, uint32_t V, uint32_t* core_out, uint32_t* kmax) {
+    if (V && (!off || !core_out || (off[V] && !nbr))) { set_error_msg("null argument"); return KC_ERR_INVALID; }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(g_oneshot_mu);
+    if ((int)g_oneshot.size() <= dev) g_oneshot.resize(dev + 1, nullptr);
+    if (!g_oneshot[dev]) {
+        int rc = graph_create(&g_oneshot[dev]);
+        if (rc) return rc;
+    }
+    kc_graph* g = g_oneshot[dev];
+    int rc = graph_load(g, off, nbr, V);
+    if (rc) return rc;
+    rc = graph_launch(g, false);
+    if (rc) return rc;
+    rc = graph_finish(g, nullptr);
+    if (rc) return rc;
+    if (V) KC_CUDA(cudaMemcpyAsync(core_out, g->d_core, sizeof(uint32_t) * V, cudaMemcpyDeviceToHost, g->stream));
+    KC_CUDA(cudaStreamSynchronize(g->stream));
+    if (kmax) *kmax = g->h_ctl->kmax;
+    return KC_OK;
+}
+
+int kc_device_info(int* sms, int* grid, int* cc_major, int* cc_minor) {
+    int dev = 0, n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) { set_error_msg("no CUDA device"); return KC_ERR_NODEV; }
+    KC_CUDA(cudaGetDevice(&dev));
+    if (sms) cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cc_major) cudaDeviceGetAttribute(cc_major, cudaDevAttrComputeCapabilityMajor, dev);
+    if (cc_minor) cudaDeviceGetAttribute(cc_minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (grid) *grid = persistent_grid(dev);
+    return KC_OK;
+}
+
+void* kc_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) return nullptr;
+    return p;
+}
+
+void kc_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,145 @@
+// Device-side building blocks of the GB300 level-synchronous peel.
+//
+// Algorithm (same result as the reference's kcore(), src/ours.cc:117-160):
+// for level = 0,1,2,... every vertex whose remaining degree equals `level` is
+// peeled; peeling v decrements each neighbour u with deg[u] > level, and a
+// neighbour whose degree falls to `level` is peeled in the same level
+// (ours.cc:92-105).  When every vertex is peeled, the level at which a vertex
+// was peeled is its core number and the last level is kmax (ours.cc:151).
+//
+// GB300 design (no reference counterpart):
+//  * w[v] holds deg(v) + kBias.  Bit 31 (kClaim) marks a vertex as peeled
+//    ("claimed").  A vertex is claimed exactly once, by an atomicOr that sees
+//    the bit clear, either by the frontier scan (w == level+kBias) or by the
+//    walker whose atomicSub took w from level+1 to level (ours.cc:96).  The
+//    bias keeps transient over-decrements (stale readers that are undone, as
+//    in ours.cc:102-105) from ever borrowing into the claim bit.
+//  * Because claims are exclusive, the scan and the neighbour walk of one
+//    level run concurrently: scan hits are walked inline by the scanning warp,
+//    cascades go to a warp-local list, and only hubs (> kLocalArcs arcs) and
+//    list overflow go to a global queue of arc-range tasks.  There is no grid
+//    barrier inside a level; a level ends when every CTA has finished its scan
+//    slice and every queued task is done, which the last event detects and
+//    publishes by atomicMax on `levels_done`.
+//  * Every wait is bounded (spin_limit); on expiry the kernel records
+//    KC_ERR_TIMEOUT and returns instead of trapping.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kc {
+
+constexpr uint32_t kBias = 1u << 30;
+constexpr uint32_t kClaim = 1u << 31;
+constexpr uint32_t kItemCap = 128;    // per-warp batch of arc ranges
+constexpr uint32_t kLocalArcs = 256;  // vertices with more arcs go to the task queue
+constexpr uint32_t kChunk = 256;      // arcs per queued task (len-1 fits 8 bits)
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+// Device status codes (mirrors of KC_ERR_*; 0 = ok).
+constexpr int kErrOverflow = -4;
+constexpr int kErrTimeout = -5;
+
+// Counters of one level.  A ring of 4 slots is reused: CTA 0 clears the slot
+// of level L-2 when it starts level L, when no warp can still touch it.
+struct alignas(128) LevelSlot {
+    unsigned int tail;  // tasks pushed in this level
+    unsigned int head;  // tasks claimed
+    unsigned int pad0[30];
+    unsigned int done;      // tasks completed
+    unsigned int arrivals;  // CTAs that finished scan + inline walk
+    unsigned int pad1[30];
+};
+
+struct alignas(128) PeelCtl {
+    LevelSlot slot[4];
+    unsigned int levels_done;  // atomicMax(level+1) when a level is complete
+    unsigned int pad0[31];
+    unsigned int peeled;       // vertices claimed so far
+    unsigned int order_tail;   // next peel-order position
+    unsigned int pad1[30];
+    int err;                   // first error (0 = ok)
+    unsigned int err_level;
+    unsigned int kmax;
+    unsigned int levels;
+    unsigned long long tasks;  // tasks pushed (stats)
+    unsigned int pad2[26];
+};
+
+struct PeelArgs {
+    const uint32_t* off;        // V+1 arc offsets
+    const uint32_t* nbr;        // arcs
+    uint32_t* w;                // working state, roundup(V,128) entries, 16-B aligned
+    uint32_t* core;             // out: core number per vertex
+    uint32_t* order;            // optional out: vertices in peel order
+    uint32_t* shells;           // optional out: k-shell offsets into order
+    unsigned long long* tasks;  // task queue storage
+    PeelCtl* ctl;
+    unsigned long long task_cap;
+    uint32_t V;
+    uint32_t shell_cap;
+    uint32_t max_level;         // max degree: no vertex survives past it
+    uint32_t epoch;             // 1..255, tags this run's task entries
+    uint32_t spin_limit;        // bounded waits
+};
+
+// ---------------------------------------------------------------- memory ops
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned ld_relaxed(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ int ld_err(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Task entry: [63:32] first arc | [31:24] len-1 | [23:8] level | [7:0] epoch.
+__device__ __forceinline__ unsigned long long make_task(uint32_t start, uint32_t len, uint32_t level,
+                                                        uint32_t epoch) {
+    return ((unsigned long long)start << 32) | ((unsigned long long)(len - 1) << 24) |
+           ((unsigned long long)(level & 0xFFFF) << 8) | (epoch & 0xFF);
+}
+__device__ __forceinline__ bool task_ready(unsigned long long e, uint32_t level, uint32_t epoch) {
+    return (uint32_t)(e & 0xFFFFFF) == (((level & 0xFFFF) << 8) | (epoch & 0xFF));
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Warp-wide exclusive prefix sum; *total receives the sum.
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t* total) {
+    const unsigned lane = lane_id();
+    uint32_t inc = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t y = __shfl_up_sync(kFull, inc, d);
+        if (lane >= (unsigned)d) inc += y;
+    }
+    *total = __shfl_sync(kFull, inc, 31);
+    return inc - x;
+}
+
+__device__ __forceinline__ void record_error(PeelCtl* ctl, int code, uint32_t level) {
+    if (atomicCAS(&ctl->err, 0, code) == 0) ctl->err_level = level;
+}
+
+}  // namespace kc
