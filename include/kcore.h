@@ -111,7 +111,8 @@ int  kc_write_edgelist(const char* path, const uint32_t* src, const uint32_t* ds
 typedef struct kc_stats {
     uint32_t V;
     uint32_t kmax;         /* degeneracy = level-1 at loop exit (ours.cc:151)    */
-    uint32_t levels;       /* level iterations run = kmax+1                      */
+    uint32_t levels;       /* levels of the reference loop = kmax+1              */
+    uint32_t iterations;   /* level iterations run (runs of empty levels skipped) */
     uint32_t blocks;       /* persistent CTAs launched                           */
     uint64_t arcs;         /* offsets[V]                                         */
     uint64_t tasks;        /* hub chunks / spilled vertices pushed to the queue  */
@@ -140,6 +141,12 @@ int  kc_peel(kc_graph* g, uint32_t* core_out, uint32_t* kmax, kc_stats* st);
 int  kc_degeneracy_order(kc_graph* g, uint32_t* order_out,
                          uint32_t* shell_offsets_out, uint32_t shell_cap,
                          uint32_t* kmax);
+/* Tracing: runs a peel that records per-level device timestamps (ns of
+ * %globaltimer) and counters, 6 words per level iteration: start, CTA 0
+ * arrival, announced complete, CTA 0 saw completion, vertices peeled so far,
+ * last CTA arrival.  out holds level_cap*6 words; *levels = iterations run.  (The
+ * reference's per-level trace is a commented-out cout, src/ours.cc:148.)       */
+int  kc_graph_trace(kc_graph* g, uint64_t* out, uint32_t level_cap, uint32_t* levels);
 /* Device pointers of the resident CSR/core arrays (for zero-copy consumers).     */
 int  kc_graph_device_ptrs(kc_graph* g, const uint32_t** d_offsets,
                           const uint32_t** d_neighbors, uint32_t** d_core);

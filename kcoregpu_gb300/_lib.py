@@ -37,7 +37,7 @@ class CsrHost(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [("V", C.c_uint32), ("kmax", C.c_uint32), ("levels", C.c_uint32),
-                ("blocks", C.c_uint32), ("arcs", C.c_uint64), ("tasks", C.c_uint64),
+                ("iterations", C.c_uint32), ("blocks", C.c_uint32), ("arcs", C.c_uint64), ("tasks", C.c_uint64),
                 ("peel_ms", C.c_float), ("total_ms", C.c_float)]
 
     def as_dict(self) -> dict:
@@ -76,6 +76,7 @@ SIGNATURES = {
     "kc_graph_fetch": (C.c_int, [_vp, _u32p, _u32p, C.POINTER(Stats)]),
     "kc_peel": (C.c_int, [_vp, _u32p, _u32p, C.POINTER(Stats)]),
     "kc_degeneracy_order": (C.c_int, [_vp, _u32p, _u32p, C.c_uint32, _u32p]),
+    "kc_graph_trace": (C.c_int, [_vp, _u64p, C.c_uint32, _u32p]),
     "kc_graph_device_ptrs": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
     "kc_graph_free": (None, [_vp]),
     "kc_peel_csr": (C.c_int, [_u32p, _u32p, C.c_uint32, _u32p, _u32p]),

@@ -30,6 +30,7 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", f"-I{INCLUDE}", 
 
 CU_SOURCES = ["kc_peel.cu", "kc_api.cu", "kc_batch.cu", "kc_serve.cu"]
 CXX_SOURCES = ["kc_host.cpp", "kc_gen.cpp"]
+CHECKED_SOURCES = ["kc_peel.cu"]
 
 
 def _nvcc() -> str:
@@ -66,6 +67,12 @@ def build_library(force: bool = False) -> Path:
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             jobs.append([nvcc] + NVCC_FLAGS + ["-c", str(src), "-o", str(obj)])
+    for s in CHECKED_SOURCES:   # bounds-checked second instantiation (KC_CHECKED=1)
+        src = CSRC / s
+        obj = BUILD / (s + ".checked.o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + headers):
+            jobs.append([nvcc] + NVCC_FLAGS + ["-DKC_CHECKED", "-c", str(src), "-o", str(obj)])
     for s in CXX_SOURCES:
         src = CSRC / s
         obj = BUILD / (s + ".o")

@@ -4,6 +4,7 @@
 // device memory glue (src/gpu_memory_allocation.cu:4-22).
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -30,6 +31,17 @@ int cuda_fail(cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
+// The bounds-checked kernel variant is used when KC_CHECKED=1 is set.
+static bool checked_mode() {
+    static const bool on = [] {
+        const char* e = std::getenv("KC_CHECKED");
+        return e && e[0] == '1';
+    }();
+    return on;
+}
+
+static const void* peel_kernel() { return checked_mode() ? peel_persistent_fn_checked() : peel_persistent_fn(); }
+
 // Persistent grid size per device: SMs x co-resident CTAs.
 static int persistent_grid(int dev) {
     static std::mutex mu;
@@ -39,7 +51,7 @@ static int persistent_grid(int dev) {
     if (cache[dev]) return cache[dev];
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_persistent_fn(), kPeelThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_kernel(), kPeelThreads, 0);
     if (per < 1) per = 1;
     cache[dev] = sms * per;
     return cache[dev];
@@ -68,6 +80,7 @@ struct kc_graph {
     unsigned long long task_cap = 0;
     PeelCtl* d_ctl = nullptr;
     PeelCtl* h_ctl = nullptr;   // pinned
+    PeelCtl* h_ctl_init = nullptr;   // pinned initial image (slot minima = none)
     uint32_t epoch = 0;
     int grid = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -75,6 +88,9 @@ struct kc_graph {
     bool ran = false;
     bool with_order = false;
     uint32_t shell_cap = 0;
+    unsigned long long* d_trace = nullptr;
+    uint32_t trace_cap = 0;
+    uint32_t* d_alive[2] = {nullptr, nullptr};   // alive-vertex lists (scratch)
 };
 
 namespace {
@@ -85,7 +101,10 @@ void release(kc_graph* g) {
     if (g->stream) cudaStreamSynchronize(g->stream);
     cudaFree(g->d_off); cudaFree(g->d_nbr); cudaFree(g->d_w); cudaFree(g->d_core);
     cudaFree(g->d_order); cudaFree(g->d_shells); cudaFree(g->d_tasks); cudaFree(g->d_ctl);
+    cudaFree(g->d_trace);
+    cudaFree(g->d_alive[0]); cudaFree(g->d_alive[1]);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
+    if (g->h_ctl_init) cudaFreeHost(g->h_ctl_init);
     if (g->ev0) cudaEventDestroy(g->ev0);
     if (g->ev1) cudaEventDestroy(g->ev1);
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
@@ -98,11 +117,14 @@ int reserve(kc_graph* g, uint32_t V, uint64_t E) {
     const uint32_t Vpad = (V + 127u) / 128u * 128u;
     if (V > g->cap_V || !g->d_off) {
         cudaFree(g->d_off); cudaFree(g->d_w); cudaFree(g->d_core); cudaFree(g->d_order);
-        cudaFree(g->d_shells);
+        cudaFree(g->d_shells); cudaFree(g->d_alive[0]); cudaFree(g->d_alive[1]);
         g->d_off = g->d_w = g->d_core = g->d_order = g->d_shells = nullptr;
+        g->d_alive[0] = g->d_alive[1] = nullptr;
         KC_CUDA(cudaMalloc(&g->d_off, sizeof(uint32_t) * ((size_t)Vpad + 4)));
         KC_CUDA(cudaMalloc(&g->d_w, sizeof(uint32_t) * ((size_t)Vpad + 4)));
         KC_CUDA(cudaMalloc(&g->d_core, sizeof(uint32_t) * ((size_t)Vpad + 4)));
+        KC_CUDA(cudaMalloc(&g->d_alive[0], sizeof(uint32_t) * ((size_t)Vpad + 4)));
+        KC_CUDA(cudaMalloc(&g->d_alive[1], sizeof(uint32_t) * ((size_t)Vpad + 4)));
         g->cap_V = V;
     }
     if (E > g->cap_E || !g->d_nbr) {
@@ -139,6 +161,9 @@ int graph_create(kc_graph** out) {
     KC_CUDA(cudaMalloc(&g->d_ctl, sizeof(PeelCtl)));
     KC_CUDA(cudaMallocHost(&g->h_ctl, sizeof(PeelCtl)));
     std::memset(g->h_ctl, 0, sizeof(PeelCtl));
+    KC_CUDA(cudaMallocHost(&g->h_ctl_init, sizeof(PeelCtl)));
+    std::memset(g->h_ctl_init, 0, sizeof(PeelCtl));
+    for (auto& sl : g->h_ctl_init->slot) sl.min_next = 0xFFFFFFFFu;
     g->grid = persistent_grid(g->dev);
     *out = g;
     return KC_OK;
@@ -170,7 +195,7 @@ int graph_load(kc_graph* g, const uint32_t* off, const uint32_t* nbr, uint32_t V
     return KC_OK;
 }
 
-int graph_launch(kc_graph* g, bool with_order) {
+int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     KC_CUDA(cudaSetDevice(g->dev));
     g->with_order = with_order;
     if (g->V == 0) {   // the reference loop never runs: kmax = level-1 = 0xFFFFFFFF
@@ -193,10 +218,20 @@ int graph_launch(kc_graph* g, bool with_order) {
             g->shell_cap = sc;
         }
     }
+    if (with_trace) {
+        const uint32_t tc = g->maxdeg + 2;
+        if (!g->d_trace || tc > g->trace_cap) {
+            cudaFree(g->d_trace);
+            g->d_trace = nullptr;
+            KC_CUDA(cudaMalloc(&g->d_trace, sizeof(unsigned long long) * kTraceFields * tc));
+            g->trace_cap = tc;
+        }
+        KC_CUDA(cudaMemsetAsync(g->d_trace, 0, sizeof(unsigned long long) * kTraceFields * g->trace_cap, g->stream));
+    }
     g->epoch = g->epoch % 255u + 1u;
     if (g->epoch == 1u)
         KC_CUDA(cudaMemsetAsync(g->d_tasks, 0, sizeof(unsigned long long) * g->task_cap, g->stream));
-    KC_CUDA(cudaMemsetAsync(g->d_ctl, 0, sizeof(PeelCtl), g->stream));
+    KC_CUDA(cudaMemcpyAsync(g->d_ctl, g->h_ctl_init, sizeof(PeelCtl), cudaMemcpyHostToDevice, g->stream));
     PeelArgs a;
     a.off = g->d_off;
     a.nbr = g->d_nbr;
@@ -212,9 +247,14 @@ int graph_launch(kc_graph* g, bool with_order) {
     a.max_level = g->maxdeg;
     a.epoch = g->epoch;
     a.spin_limit = 1u << 22;
+    a.E = (uint32_t)g->E;
+    a.alive[0] = g->d_alive[0];
+    a.alive[1] = g->d_alive[1];
+    a.trace = with_trace ? g->d_trace : nullptr;
+    a.trace_cap = with_trace ? g->trace_cap : 0;
     void* args[] = {&a};
     KC_CUDA(cudaEventRecord(g->ev0, g->stream));
-    KC_CUDA(cudaLaunchCooperativeKernel(peel_persistent_fn(), dim3(g->grid), dim3(kPeelThreads), args, 0, g->stream));
+    KC_CUDA(cudaLaunchCooperativeKernel(peel_kernel(), dim3(g->grid), dim3(kPeelThreads), args, 0, g->stream));
     KC_CUDA(cudaEventRecord(g->ev1, g->stream));
     KC_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(PeelCtl), cudaMemcpyDeviceToHost, g->stream));
     g->pending = true;
@@ -228,8 +268,12 @@ int graph_finish(kc_graph* g, kc_stats* st) {
     KC_CUDA(cudaStreamSynchronize(g->stream));
     g->pending = false;
     if (g->h_ctl->err) {
-        set_error_msg(std::string("device peel failed at level ") + std::to_string(g->h_ctl->err_level));
-        return g->h_ctl->err;
+        std::string m = std::string("device peel failed at level ") + std::to_string(g->h_ctl->err_level);
+        if (g->h_ctl->err == kErrCheck)
+            m += ": out-of-bounds index " + std::to_string(g->h_ctl->err_index) + " at access site " +
+                 std::to_string(g->h_ctl->err_site) + " (skipped)";
+        set_error_msg(m);
+        return g->h_ctl->err == kErrCheck ? KC_ERR_OVERFLOW : g->h_ctl->err;
     }
     if (st) {
         float ms = 0;
@@ -237,6 +281,7 @@ int graph_finish(kc_graph* g, kc_stats* st) {
         st->V = g->V;
         st->kmax = g->h_ctl->kmax;
         st->levels = g->h_ctl->levels;
+        st->iterations = g->h_ctl->iterations;
         st->blocks = (uint32_t)g->grid;
         st->arcs = g->E;
         st->tasks = g->h_ctl->tasks;
@@ -345,6 +390,19 @@ int kc_degeneracy_order(kc_graph* g, uint32_t* order_out, uint32_t* shells_out, 
         if (shell_cap < need) { set_error_msg("shell_offsets_out needs kmax+2 entries"); return KC_ERR_INVALID; }
         KC_CUDA(cudaMemcpy(shells_out, g->d_shells, sizeof(uint32_t) * need, cudaMemcpyDeviceToHost));
     }
+    return KC_OK;
+}
+
+int kc_graph_trace(kc_graph* g, uint64_t* out, uint32_t level_cap, uint32_t* levels) {
+    if (!g || !out) return KC_ERR_INVALID;
+    int rc = graph_launch(g, false, true);
+    if (rc) return rc;
+    rc = graph_finish(g, nullptr);
+    if (rc) return rc;
+    const uint32_t lv = g->h_ctl->iterations;
+    if (levels) *levels = lv;
+    const uint32_t n = std::min(lv, level_cap);
+    if (n) KC_CUDA(cudaMemcpy(out, g->d_trace, sizeof(uint64_t) * kTraceFields * n, cudaMemcpyDeviceToHost));
     return KC_OK;
 }
 

@@ -39,31 +39,40 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 // Device status codes (mirrors of KC_ERR_*; 0 = ok).
 constexpr int kErrOverflow = -4;
 constexpr int kErrTimeout = -5;
+constexpr int kErrCheck = -12;   // checked build: an index was out of bounds (access skipped)
 
-// Counters of one level.  A ring of 4 slots is reused: CTA 0 clears the slot
-// of level L-2 when it starts level L, when no warp can still touch it.
+// Counters of one level iteration.  A ring of 4 slots is reused: CTA 0 clears
+// the slot of iteration i-2 when it starts iteration i, when no warp can still
+// touch it.  The 64-bit words pack a count in the high half with the vertices
+// peeled by that event in the low half, so one atomic publishes both.
 struct alignas(128) LevelSlot {
     unsigned int tail;  // tasks pushed in this level
     unsigned int head;  // tasks claimed
     unsigned int pad0[30];
-    unsigned int done;      // tasks completed
-    unsigned int arrivals;  // CTAs that finished scan + inline walk
+    unsigned long long done_peel;  // [63:32] tasks completed, [31:0] vertices they claimed
     unsigned int pad1[30];
+    unsigned long long arr_peel;   // [63:32] CTAs arrived, [31:0] vertices their scans claimed
+    unsigned int pad2[30];
+    unsigned int alive_next;  // survivors appended to the next alive list
+    unsigned int min_next;    // smallest survivor state seen by the scans (0xFFFFFFFF = none)
+    unsigned int pad3[30];
 };
 
 struct alignas(128) PeelCtl {
     LevelSlot slot[4];
-    unsigned int levels_done;  // atomicMax(level+1) when a level is complete
+    unsigned int iters_done;   // atomicMax(iteration+1) when an iteration is complete
     unsigned int pad0[31];
-    unsigned int peeled;       // vertices claimed so far
     unsigned int order_tail;   // next peel-order position
-    unsigned int pad1[30];
+    unsigned int pad1[31];
     int err;                   // first error (0 = ok)
     unsigned int err_level;
     unsigned int kmax;
-    unsigned int levels;
+    unsigned int levels;       // kmax + 1, as the reference counts them
     unsigned long long tasks;  // tasks pushed (stats)
-    unsigned int pad2[26];
+    unsigned int err_site;     // checked build: access site of the first violation
+    unsigned int iterations;   // level iterations actually run (empty runs skipped)
+    unsigned long long err_index;   // checked build: its index
+    unsigned int pad2[22];
 };
 
 struct PeelArgs {
@@ -81,7 +90,15 @@ struct PeelArgs {
     uint32_t max_level;         // max degree: no vertex survives past it
     uint32_t epoch;             // 1..255, tags this run's task entries
     uint32_t spin_limit;        // bounded waits
+    unsigned long long* trace;  // optional per-level timestamps (kTraceFields per level)
+    uint32_t trace_cap;         // levels the trace buffer holds
+    uint32_t* alive[2];         // optional alive-vertex lists (roundup(V,128) each); null = dense scans only
+    uint32_t E;                 // arcs (= off[V])
 };
+
+// Per-level trace words: level start (CTA 0), CTA 0 arrival, level announced
+// complete, CTA 0 saw completion, vertices peeled so far, last CTA arrival.
+constexpr int kTraceFields = 6;
 
 // ---------------------------------------------------------------- memory ops
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -94,6 +111,11 @@ __device__ __forceinline__ unsigned ld_relaxed(const unsigned* p) {
     asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ unsigned long long ld_acquire64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long* p) {
     unsigned long long v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -102,6 +124,7 @@ __device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long l
 __device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned long long v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+__device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ int ld_err(const int* p) {
     int v;
     asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -141,5 +164,24 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t x, uint32_t* total) 
 __device__ __forceinline__ void record_error(PeelCtl* ctl, int code, uint32_t level) {
     if (atomicCAS(&ctl->err, 0, code) == 0) ctl->err_level = level;
 }
+
+// Bounds check of the checked build (compiled with KC_CHECKED): records the
+// first out-of-bounds index with its access site and level, and tells the
+// caller to skip the access.  In the normal build it is a constant true.
+#ifdef KC_CHECKED
+static __device__ __noinline__ bool kc_in_bounds_fail(PeelCtl* ctl, unsigned long long idx, int site, uint32_t level) {
+    if (atomicCAS(&ctl->err, 0, kErrCheck) == 0) {
+        ctl->err_level = level;
+        ctl->err_site = (unsigned)site;
+        ctl->err_index = idx;
+    }
+    return false;
+}
+#define KC_IN(ctl, idx, size, site, level)                                                          \
+    (((unsigned long long)(idx) < (unsigned long long)(size)) ? true                                \
+                                                                : kc_in_bounds_fail((ctl), (idx), (site), (level)))
+#else
+#define KC_IN(ctl, idx, size, site, level) true
+#endif
 
 }  // namespace kc

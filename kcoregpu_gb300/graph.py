@@ -150,6 +150,17 @@ class DeviceGraph:
         nsh = 1 if self.V == 0 else k + 2
         return order[: self.V], shells[:nsh], k
 
+    def trace(self):
+        """Per-level device trace -> (levels x 6) uint64 array: level start,
+        CTA 0 arrival, level complete, CTA 0 saw completion (ns), vertices
+        peeled so far, last CTA arrival (ns)."""
+        maxdeg = int(np.diff(self.offsets).max()) if self.V else 0
+        buf = np.zeros((maxdeg + 2) * 6, np.uint64)
+        lv = C.c_uint32()
+        check(lib().kc_graph_trace(self._h, buf.ctypes.data_as(C.POINTER(C.c_uint64)), maxdeg + 2,
+                                   C.byref(lv)), "kc_graph_trace")
+        return buf.reshape(-1, 6)[: lv.value]
+
     def free(self) -> None:
         if getattr(self, "_h", None):
             lib().kc_graph_free(self._h)

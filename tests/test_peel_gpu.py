@@ -127,3 +127,21 @@ def test_full_size_workloads(gpu, cfg):
     src = np.repeat(np.arange(len(deg)), deg)
     strong = np.bincount(src[core[nbr] >= core[src]], minlength=len(deg))
     assert (strong >= core).all()
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("cfg", [2, 3])
+def test_repeated_full_size_peels_are_stable(gpu, cfg):
+    # Every repetition must reproduce the oracle: a race in the level
+    # completion protocol shows up here as a wrong core number.
+    from kcoregpu_gb300 import workloads
+    off, nbr = workloads.single_graph(cfg)
+    want, wk = O.bz(off, nbr)
+    g = kc.DeviceGraph(off, nbr)
+    for _ in range(25):
+        core, kmax, _ = g.peel()
+        np.testing.assert_array_equal(core, want)
+        assert kmax == wk
+    tr = g.trace()
+    assert 1 <= len(tr) <= wk + 1 and int(tr[-1, 4]) == len(off) - 1
+    g.free()
