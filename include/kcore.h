@@ -157,6 +157,23 @@ void kc_graph_free(kc_graph* g);
 int  kc_peel_csr(const uint32_t* offsets, const uint32_t* neighbors, uint32_t V,
                  uint32_t* core_out, uint32_t* kmax);
 
+/* ---- allocation-free single-graph peel (no counterpart in the reference) ----
+ * For callers that cannot call cudaMalloc: a plugin whose host application owns
+ * all device memory through its own pool, or a latency-critical loop where an
+ * allocation would add allocator latency and device-wide synchronisation.  The
+ * caller passes device buffers: offsets (V+1), neighbors (n_arcs), core_out
+ * (V); kmax is copied to the host pointer kmax_out (may be NULL).  The call
+ * allocates nothing: its scratch is one static device array sized for
+ * V <= KC_NOALLOC_MAX_V and n_arcs <= KC_NOALLOC_MAX_ARCS (larger graphs are
+ * rejected with KC_ERR_INVALID), held by every GPU that loads the library until
+ * exit.  The first call on a device resolves that array's address; make it
+ * before any stream capture.  All calls on a device share the array: calls
+ * that overlap on the GPU race, so serialise them.  Returns when done.        */
+#define KC_NOALLOC_MAX_V     524288u
+#define KC_NOALLOC_MAX_ARCS  8388608u
+int  kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neighbors, uint32_t V,
+                     uint32_t n_arcs, uint32_t* d_core_out, uint32_t* kmax_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

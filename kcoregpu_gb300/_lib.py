@@ -80,6 +80,7 @@ SIGNATURES = {
     "kc_graph_device_ptrs": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
     "kc_graph_free": (None, [_vp]),
     "kc_peel_csr": (C.c_int, [_u32p, _u32p, C.c_uint32, _u32p, _u32p]),
+    "kc_peel_noalloc": (C.c_int, [_vp, _vp, C.c_uint32, C.c_uint32, _vp, _u32p, _vp]),
 }
 
 _lib = None

@@ -1,0 +1,55 @@
+"""The allocation-free peel, kc_peel_noalloc, through the C ABI.
+
+It exists for callers that cannot call cudaMalloc (a plugin host that owns all
+device memory through its own pool, a latency-critical loop that must not pay
+for allocation and the device-wide synchronisation it brings).  The test plays
+such a caller: it owns the device buffers (allocated here with torch), hands
+them to the entry point, and checks the core numbers and kmax of two calls in
+a row, on two different graphs, bit for bit against the allocating entry point
+kc_peel_csr.  The second call also shows that the shared scratch is reset
+between calls.  This file sorts last so that a run stopping at its first
+failure has already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import kcoregpu_gb300 as kc
+from kcoregpu_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc_peel(torch, off, nbr):
+    lib = kc.lib()
+    V = len(off) - 1
+    d_off = torch.from_numpy(off.view(np.int32)).cuda()
+    d_nbr = torch.from_numpy(nbr.view(np.int32)).cuda()
+    d_core = torch.full((max(V, 1),), -1, dtype=torch.int32, device="cuda")
+    kmax = C.c_uint32(12345)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.kc_peel_noalloc(C.c_void_p(d_off.data_ptr()), C.c_void_p(d_nbr.data_ptr()), V, len(nbr),
+                             C.c_void_p(d_core.data_ptr()), C.byref(kmax), C.c_void_p(stream))
+    _lib.check(rc, "kc_peel_noalloc")
+    return d_core[:V].cpu().numpy().view(np.uint32), kmax.value
+
+
+def test_noalloc_matches_allocating_entry_point_on_two_calls(gpu):
+    torch = pytest.importorskip("torch")
+    graphs = [kc.build_csr(*kc.gen_rmat(300_000, 2_000_000, seed=21))[:2],
+              kc.build_csr(*kc.gen_chung_lu(400_000, 1_500_000, 2.1, 20_000.0, seed=22))[:2]]
+    for off, nbr in graphs:   # two calls in a row on the shared scratch
+        assert len(off) - 1 <= 524288 and len(nbr) <= 8388608   # KC_NOALLOC_MAX_V / _ARCS
+        want, wk = kc.peel_csr(off, nbr)
+        got, gk = _noalloc_peel(torch, off, nbr)
+        np.testing.assert_array_equal(got, want)
+        assert gk == wk
+
+
+def test_noalloc_rejects_graphs_beyond_its_limit(gpu):
+    lib = kc.lib()
+    kmax = C.c_uint32()
+    rc = lib.kc_peel_noalloc(None, None, 524288 + 1, 0, None, C.byref(kmax), None)
+    assert _lib.ERRORS[rc] == "KC_ERR_INVALID"
+    assert b"scratch limits" in lib.kc_last_error()
