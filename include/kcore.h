@@ -157,6 +157,66 @@ void kc_graph_free(kc_graph* g);
 int  kc_peel_csr(const uint32_t* offsets, const uint32_t* neighbors, uint32_t V,
                  uint32_t* core_out, uint32_t* kmax);
 
+/* ---- batched peel: many independent graphs in one persistent launch ----
+ * No reference counterpart (the reference peels one graph per process).  The
+ * graphs are packed as one segmented CSR with graph-local uint32 ids and
+ * offsets and 64-bit per-graph bases.                                          */
+typedef struct kc_segcsr {
+    uint32_t        ngraphs;
+    const uint64_t* vbase;      /* ngraphs+1: first vertex of graph g (prefix of V_g)  */
+    const uint64_t* abase;      /* ngraphs+1: first arc of graph g (prefix of E_g)     */
+    const uint32_t* offsets;    /* graph g: V_g+1 local offsets at vbase[g]+g          */
+    const uint32_t* neighbors;  /* graph g: E_g local neighbour ids at abase[g]        */
+} kc_segcsr;
+
+typedef struct kc_segcsr_host {   /* library-owned segmented CSR (kc_gen_batch)     */
+    uint32_t  ngraphs;
+    uint64_t* vbase;
+    uint64_t* abase;
+    uint32_t* offsets;
+    uint32_t* neighbors;
+} kc_segcsr_host;
+
+typedef struct kc_batch_stats {
+    uint32_t ngraphs;
+    uint32_t giants;      /* graphs the autotuner sent to the grid-wide peel      */
+    uint32_t blocks;      /* CTAs of the batched kernel                           */
+    uint32_t qcap;        /* per-CTA queue entries (largest batched graph)        */
+    uint64_t V_total;
+    uint64_t arcs_total;
+    float    peel_ms;     /* device time of the whole batch (CUDA events)         */
+} kc_batch_stats;
+
+typedef struct kc_batch kc_batch;
+
+/* Uploads a segmented CSR and runs the autotuner: per-graph cost from the
+ * degree histogram (V, E, max degree, h-index), largest-first schedule over the
+ * CTAs, graphs too large for one CTA routed to the grid-wide peel, per-CTA
+ * queue size and CTAs per SM.                                                  */
+int  kc_batch_upload(const kc_segcsr* graphs, kc_batch** b);
+int  kc_batch_set_stream(kc_batch* b, void* stream);
+/* One persistent launch over all graphs (plus one grid-wide launch per giant). */
+int  kc_batch_peel_async(kc_batch* b);
+/* Waits; copies core numbers (sum of V_g, graph g at vbase[g]) and per-graph
+ * kmax (ngraphs) to the host; either may be NULL.                             */
+int  kc_batch_fetch(kc_batch* b, uint32_t* core_out, uint32_t* kmax_out, kc_batch_stats* st);
+/* Baseline: the plain single-graph peel launched once per graph, back to back
+ * on the stream; results land in the same buffers.  *ms_out = device time.    */
+int  kc_batch_peel_per_graph(kc_batch* b, float* ms_out);
+/* The autotuner's plan: giants first, then the batched schedule (ngraphs ids). */
+int  kc_batch_plan(kc_batch* b, uint32_t* schedule_out, uint32_t* ngiants, uint32_t* qcap,
+                   uint32_t* blocks);
+void kc_batch_free(kc_batch* b);
+/* One-shot: upload, peel, fetch, free.                                         */
+int  kc_batch_peel(const kc_segcsr* graphs, uint32_t* core_out, uint32_t* kmax_out,
+                   kc_batch_stats* st);
+/* Batch generator: graph g uses seed seed_base+g, n ~ log-uniform[nmin,nmax],
+ * average degree 2m/n ~ U[dmin,dmax]; even g Erdos-Renyi G(n,m), odd g R-MAT
+ * (a,b,c) with m draws; each graph deduplicated/symmetrised as kc_build_csr.   */
+int  kc_gen_batch(uint32_t ngraphs, uint64_t seed_base, uint32_t nmin, uint32_t nmax,
+                  double dmin, double dmax, double a, double b, double c, kc_segcsr_host* out);
+void kc_segcsr_free(kc_segcsr_host* s);
+
 /* ---- allocation-free single-graph peel (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc: a plugin whose host application owns
  * all device memory through its own pool, or a latency-critical loop where an

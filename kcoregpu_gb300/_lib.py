@@ -49,6 +49,20 @@ _u64p = C.POINTER(C.c_uint64)
 _vp = C.c_void_p
 _cp = C.c_char_p
 
+
+class SegCsr(C.Structure):
+    _fields_ = [("ngraphs", C.c_uint32), ("vbase", _u64p), ("abase", _u64p),
+                ("offsets", _u32p), ("neighbors", _u32p)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("ngraphs", C.c_uint32), ("giants", C.c_uint32), ("blocks", C.c_uint32),
+                ("qcap", C.c_uint32), ("V_total", C.c_uint64), ("arcs_total", C.c_uint64),
+                ("peel_ms", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
 # name -> (restype, argtypes); every entry is declared in include/kcore.h
 SIGNATURES = {
     "kc_strerror": (C.c_char_p, [C.c_int]),
@@ -81,6 +95,17 @@ SIGNATURES = {
     "kc_graph_free": (None, [_vp]),
     "kc_peel_csr": (C.c_int, [_u32p, _u32p, C.c_uint32, _u32p, _u32p]),
     "kc_peel_noalloc": (C.c_int, [_vp, _vp, C.c_uint32, C.c_uint32, _vp, _u32p, _vp]),
+    "kc_batch_upload": (C.c_int, [C.POINTER(SegCsr), C.POINTER(_vp)]),
+    "kc_batch_set_stream": (C.c_int, [_vp, _vp]),
+    "kc_batch_peel_async": (C.c_int, [_vp]),
+    "kc_batch_fetch": (C.c_int, [_vp, _u32p, _u32p, C.POINTER(BatchStats)]),
+    "kc_batch_peel_per_graph": (C.c_int, [_vp, C.POINTER(C.c_float)]),
+    "kc_batch_plan": (C.c_int, [_vp, _u32p, _u32p, _u32p, _u32p]),
+    "kc_batch_free": (None, [_vp]),
+    "kc_batch_peel": (C.c_int, [C.POINTER(SegCsr), _u32p, _u32p, C.POINTER(BatchStats)]),
+    "kc_gen_batch": (C.c_int, [C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_double, C.c_double,
+                               C.c_double, C.c_double, C.c_double, C.POINTER(SegCsr)]),
+    "kc_segcsr_free": (None, [C.POINTER(SegCsr)]),
 }
 
 _lib = None

@@ -38,3 +38,25 @@ def algorithmic_bytes(V: int, arcs: int, kmax: int) -> int:
     """Bytes of one level-synchronous peel: offsets once, each arc once per
     peeled endpoint, one degree-array pass per level (kmax+1 levels)."""
     return 4 * (V + 1) + 4 * arcs + 4 * V * (kmax + 1)
+
+
+BATCH = dict(name="batch-4096-er-rmat", ngraphs=4096, seed_base=1000, nmin=1000, nmax=200_000,
+             dmin=4.0, dmax=32.0)
+
+
+def batch(ngraphs: int | None = None):
+    """The batched workload: graph g uses seed 1000+g, n ~ log-uniform[1,000,
+    200,000], average degree 2m/n ~ U[4,32], even g Erdos-Renyi, odd g R-MAT."""
+    from .batch import gen_batch
+    c = BATCH
+    return gen_batch(ngraphs or c["ngraphs"], c["seed_base"], c["nmin"], c["nmax"], c["dmin"], c["dmax"])
+
+
+def batch_algorithmic_bytes(seg, kmax) -> int:
+    """Sum over the graphs of the single-graph formula."""
+    import numpy as np
+    V = np.diff(seg.vbase).astype(np.int64)
+    A = np.diff(seg.abase).astype(np.int64)
+    k = np.asarray(kmax, dtype=np.int64)
+    k = np.where(k == 0xFFFFFFFF, -1, k)
+    return int((4 * (V + 1) + 4 * A + 4 * V * (k + 1)).sum())
