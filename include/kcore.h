@@ -217,6 +217,59 @@ int  kc_gen_batch(uint32_t ngraphs, uint64_t seed_base, uint32_t nmin, uint32_t 
                   double dmin, double dmax, double a, double b, double c, kc_segcsr_host* out);
 void kc_segcsr_free(kc_segcsr_host* s);
 
+/* ---- served peel: continuous batching of k-core requests ----
+ * No reference counterpart.  A request loop admits submitted graphs against an
+ * HBM budget (first come, first served), uploads them, and hands them to a
+ * persistent serve kernel that keeps running while requests flow: small graphs
+ * are peeled by one CTA each, large ones by a gang of CTAs (one CTA per
+ * gang_arcs arcs, up to max_gang), and requests that arrive while others run
+ * start as soon as CTAs and memory free up.  submit/poll/wait are thread-safe. */
+typedef struct kc_serve_cfg {
+    uint64_t hbm_budget_bytes;   /* device memory the admitted requests may hold (0: 64 GiB) */
+    uint32_t ring_slots;         /* max requests admitted at once (0: 1024)              */
+    uint32_t gang_arcs;          /* arcs per gang CTA (0: 2^21)                           */
+    uint32_t max_gang;           /* largest gang (0: every CTA of the kernel)             */
+    uint32_t small_vertices;     /* largest graph one CTA may peel alone (0: 2^18)        */
+} kc_serve_cfg;
+
+typedef struct kc_serve_timing {
+    double   queue_us;           /* submit -> admitted                                   */
+    double   latency_us;         /* submit -> core numbers on the host                   */
+    uint32_t gang;               /* CTAs that peeled it                                  */
+    uint32_t iterations;         /* level iterations run                                 */
+} kc_serve_timing;
+
+typedef struct kc_serve_stats {
+    uint64_t submitted;
+    uint64_t completed;
+    uint64_t in_use;             /* device bytes held by admitted requests now           */
+    uint64_t peak_in_use;
+    uint32_t pending;
+    uint32_t inflight;
+    uint32_t blocks;             /* CTAs of the serve kernel                             */
+    uint32_t pad;
+} kc_serve_stats;
+
+typedef struct kc_server kc_server;
+
+int  kc_serve_open(const kc_serve_cfg* cfg, kc_server** s);   /* cfg may be NULL    */
+/* Queues a CSR (host arrays that must stay valid until the request completes);
+ * the core numbers are written to core_out (V entries).  KC_ERR_BUDGET when the
+ * request alone exceeds the budget, KC_ERR_CLOSED after kc_serve_close.        */
+int  kc_serve_submit(kc_server* s, const uint32_t* offsets, const uint32_t* neighbors,
+                     uint32_t V, uint32_t* core_out, uint64_t* request_id);
+/* KC_OK (and forgets the request) once core_out holds the result, KC_ERR_BUSY
+ * while it is still queued or running.                                         */
+int  kc_serve_poll(kc_server* s, uint64_t request_id, uint32_t* kmax, kc_serve_timing* t);
+int  kc_serve_wait(kc_server* s, uint64_t request_id, uint32_t* kmax, kc_serve_timing* t,
+                   double timeout_s);
+int  kc_serve_stats_get(kc_server* s, kc_serve_stats* st);
+/* Read-only diagnostic snapshot of the server's device and host state (see
+ * kc_serve.cu for the word layout); n = capacity of out (>= 10).              */
+int  kc_serve_debug(kc_server* s, uint64_t* out, uint32_t n);
+/* Finishes the queued requests, stops the kernel and frees everything.        */
+int  kc_serve_close(kc_server* s);
+
 /* ---- allocation-free single-graph peel (no counterpart in the reference) ----
  * For callers that cannot call cudaMalloc: a plugin whose host application owns
  * all device memory through its own pool, or a latency-critical loop where an

@@ -55,6 +55,28 @@ class SegCsr(C.Structure):
                 ("offsets", _u32p), ("neighbors", _u32p)]
 
 
+class ServeCfg(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("ring_slots", C.c_uint32), ("gang_arcs", C.c_uint32),
+                ("max_gang", C.c_uint32), ("small_vertices", C.c_uint32)]
+
+
+class ServeTiming(C.Structure):
+    _fields_ = [("queue_us", C.c_double), ("latency_us", C.c_double), ("gang", C.c_uint32),
+                ("iterations", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("in_use", C.c_uint64),
+                ("peak_in_use", C.c_uint64), ("pending", C.c_uint32), ("inflight", C.c_uint32),
+                ("blocks", C.c_uint32), ("pad", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
 class BatchStats(C.Structure):
     _fields_ = [("ngraphs", C.c_uint32), ("giants", C.c_uint32), ("blocks", C.c_uint32),
                 ("qcap", C.c_uint32), ("V_total", C.c_uint64), ("arcs_total", C.c_uint64),
@@ -106,6 +128,13 @@ SIGNATURES = {
     "kc_gen_batch": (C.c_int, [C.c_uint32, C.c_uint64, C.c_uint32, C.c_uint32, C.c_double, C.c_double,
                                C.c_double, C.c_double, C.c_double, C.POINTER(SegCsr)]),
     "kc_segcsr_free": (None, [C.POINTER(SegCsr)]),
+    "kc_serve_open": (C.c_int, [C.POINTER(ServeCfg), C.POINTER(_vp)]),
+    "kc_serve_submit": (C.c_int, [_vp, _u32p, _u32p, C.c_uint32, _u32p, _u64p]),
+    "kc_serve_poll": (C.c_int, [_vp, C.c_uint64, _u32p, C.POINTER(ServeTiming)]),
+    "kc_serve_wait": (C.c_int, [_vp, C.c_uint64, _u32p, C.POINTER(ServeTiming), C.c_double]),
+    "kc_serve_stats_get": (C.c_int, [_vp, C.POINTER(ServeStats)]),
+    "kc_serve_close": (C.c_int, [_vp]),
+    "kc_serve_debug": (C.c_int, [_vp, _u64p, C.c_uint32]),
 }
 
 _lib = None

@@ -54,6 +54,12 @@ static int persistent_grid(int dev) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_kernel(), kPeelThreads, 0);
     if (per < 1) per = 1;
     cache[dev] = sms * per;
+    // KC_PEEL_GRID=n runs the persistent peel on n CTAs (n <= the co-resident
+    // maximum): the level protocol is the one gangs of the serve kernel use.
+    if (const char* e = std::getenv("KC_PEEL_GRID")) {
+        const int n = std::atoi(e);
+        if (n > 0 && n < cache[dev]) cache[dev] = n;
+    }
     return cache[dev];
 }
 
@@ -246,8 +252,9 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     a.shell_cap = with_order ? g->shell_cap : 0;
     a.max_level = g->maxdeg;
     a.epoch = g->epoch;
-    a.spin_limit = 1u << 22;
+    a.wait_us = 2000000;   // 2 s
     a.E = (uint32_t)g->E;
+    a.zero_tasks = 0;   // the queue is cleared by a memset when the tag epoch wraps
     a.alive[0] = g->d_alive[0];
     a.alive[1] = g->d_alive[1];
     a.trace = with_trace ? g->d_trace : nullptr;

@@ -175,7 +175,7 @@ int launch_single(kc_batch* b, uint32_t g) {
     a.V = p.V;
     a.max_level = p.maxdeg;
     a.epoch = b->gepoch;
-    a.spin_limit = 1u << 22;
+    a.wait_us = 2000000;   // 2 s
     a.E = (uint32_t)p.E;
     a.alive[0] = b->d_galive0;
     a.alive[1] = b->d_galive1;

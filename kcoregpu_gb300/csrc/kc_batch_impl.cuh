@@ -1,0 +1,164 @@
+// Batched peel for sm_103a: thousands of independent graphs in one persistent
+// launch.  Each CTA takes the next graph from a device work counter (graphs
+// ordered largest first by the host autotuner) and peels it alone with the
+// reference's level-synchronous method (src/ours.cc:117-160), synchronising
+// its levels and walk rounds with CTA barriers only.  A CTA owns its graph, so
+// the state array is the graph's slice of the output: when the graph is done
+// it holds the core numbers, exactly like the reference's degree array.
+#pragma once
+#include "kc_batch.cuh"
+#include "kc_device.cuh"
+
+namespace kc {
+namespace {
+
+struct BatchShared {
+    uint32_t pref[kBatchChunk + 1];  // arc prefix of the items of one walk round
+    uint32_t start[kBatchChunk];     // first arc of each item
+    uint32_t warp_tot[kBatchWarps];
+    uint32_t qtail;                  // vertices peeled so far in this graph
+    uint32_t minv;                   // smallest survivor degree seen by a level's scan
+    uint32_t g;                      // schedule index of the current graph
+};
+
+// Block-wide exclusive prefix sum of one value per thread.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, BatchShared& sh, uint32_t* total) {
+    const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t wt;
+    const uint32_t ex = warp_excl_scan(x, &wt);
+    if (lane == 0) sh.warp_tot[wid] = wt;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t t = lane < kBatchWarps ? sh.warp_tot[lane] : 0u;
+        uint32_t tt;
+        const uint32_t te = warp_excl_scan(t, &tt);
+        if (lane < kBatchWarps) sh.warp_tot[lane] = te;
+        if (lane == 0) sh.pref[kBatchChunk] = tt;   // stash the total
+    }
+    __syncthreads();
+    *total = sh.pref[kBatchChunk];
+    return sh.warp_tot[wid] + ex;
+}
+
+// Appends the vertices v of the lanes with `pred` to the CTA's queue.
+__device__ __forceinline__ void enqueue(BatchShared& sh, uint32_t* q, bool pred, uint32_t v) {
+    const unsigned m = __ballot_sync(kFull, pred);
+    if (!m) return;
+    const unsigned lane = threadIdx.x & 31;
+    uint32_t pos = 0;
+    if (lane == 0) pos = atomicAdd(&sh.qtail, (unsigned)__popc(m));
+    pos = __shfl_sync(kFull, pos, 0);
+    if (pred) q[pos + __popc(m & lanemask_lt())] = v;
+}
+
+// One neighbour u of a vertex peeled at `level` (ours.cc:91-106).  Returns
+// true when this decrement took u to the level (u joins this level).
+__device__ __forceinline__ bool step(uint32_t* w, uint32_t u, uint32_t level) {
+    if (__ldcg(w + u) <= level) return false;
+    const uint32_t old = atomicSub(w + u, 1u);
+    if (old == level + 1) return true;
+    if (old <= level) atomicAdd(w + u, 1u);   // undo (ours.cc:102-105)
+    return false;
+}
+
+// Peels one graph (V vertices, graph-local CSR off/nb) with this CTA alone.
+// w (V entries) receives the core numbers, q (>= V entries) is the CTA's
+// queue / peel order.  Thread 0 writes kmax and the level iterations run.
+__device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t* w, uint32_t V, uint32_t* q,
+                               uint32_t qcap, int* err, uint32_t* kmax_out, uint32_t* iters_out,
+                               BatchShared& sh) {
+    const unsigned tid = threadIdx.x;
+    if (V == 0) {   // the reference loop never runs: kmax = level-1 = 0xFFFFFFFF
+        if (tid == 0) { *kmax_out = 0xFFFFFFFFu; *iters_out = 0; }
+        return;
+    }
+    if (V > qcap) {
+        if (tid == 0) atomicCAS(err, 0, kErrOverflow);
+        return;
+    }
+    for (uint32_t v = tid; v < V; v += kBatchThreads) w[v] = KC_LDG(off + v + 1) - KC_LDG(off + v);
+    if (tid == 0) sh.qtail = 0;
+    __syncthreads();
+
+    uint32_t level = 0, iters = 0;
+    for (;;) {
+        if (tid == 0) sh.minv = kFull;
+        __syncthreads();
+        const uint32_t lvl_start = sh.qtail;
+        // scan: every vertex whose degree equals the level (ours.cc:15-25)
+        uint32_t mymin = kFull;
+        for (uint32_t base = 0; base < V; base += kBatchThreads) {
+            const uint32_t v = base + tid;
+            uint32_t d = kFull;
+            if (v < V) d = __ldcg(w + v);
+            if (d != kFull && d > level) mymin = min(mymin, d);
+            enqueue(sh, q, v < V && d == level, v);
+        }
+        mymin = __reduce_min_sync(kFull, mymin);
+        if ((tid & 31) == 0 && mymin != kFull) atomicMin(&sh.minv, mymin);
+        __syncthreads();
+
+        // walk rounds over the queue, including vertices appended by the walk
+        // itself (same level, ours.cc:60-107)
+        uint32_t head = lvl_start;
+        uint32_t tail = sh.qtail;
+        while (head < tail) {
+            const uint32_t n = min(tail - head, kBatchChunk);
+            uint32_t l0 = 0, l1 = 0, s0 = 0, s1 = 0;
+            const uint32_t i0 = 2 * tid, i1 = 2 * tid + 1;
+            if (i0 < n) { const uint32_t v = q[head + i0]; s0 = KC_LDG(off + v); l0 = KC_LDG(off + v + 1) - s0; }
+            if (i1 < n) { const uint32_t v = q[head + i1]; s1 = KC_LDG(off + v); l1 = KC_LDG(off + v + 1) - s1; }
+            uint32_t total;
+            const uint32_t ex = block_excl_scan(l0 + l1, sh, &total);
+            if (i0 < n) { sh.pref[i0] = ex; sh.start[i0] = s0; }
+            if (i1 < n) { sh.pref[i1] = ex + l0; sh.start[i1] = s1; }
+            __syncthreads();
+            if (tid == 0) sh.pref[n] = total;
+            __syncthreads();
+            uint32_t lo = 0;
+            for (uint32_t b = 0; b < total; b += 2 * kBatchThreads) {
+                uint32_t u[2] = {kFull, kFull};
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const uint32_t arc = b + j * kBatchThreads + tid;
+                    if (arc < total) {
+                        uint32_t hi = n;
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (sh.pref[mid] <= arc) lo = mid; else hi = mid;
+                        }
+                        u[j] = KC_LDG(nb + sh.start[lo] + (arc - sh.pref[lo]));
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    const bool f = u[j] != kFull && step(w, u[j], level);
+                    enqueue(sh, q, f, u[j]);
+                }
+            }
+            __syncthreads();
+            head += n;
+            tail = sh.qtail;
+            __syncthreads();
+        }
+        ++iters;
+        if (tail >= V) {
+            if (tid == 0) { *kmax_out = level; *iters_out = iters; }
+            return;
+        }
+        // A level that peeled nothing changed no degree: jump to the smallest
+        // survivor degree (every level in between is empty).
+        uint32_t next = level + 1;
+        const uint32_t mn = sh.minv;
+        if (tail == lvl_start && mn != kFull && mn > next) next = mn;
+        if (next > V) {   // cannot happen for a valid CSR: every vertex is peeled by its degree
+            if (tid == 0) atomicCAS(err, 0, kErrOverflow);
+            return;
+        }
+        level = next;
+        __syncthreads();
+    }
+}
+
+}  // namespace
+}  // namespace kc

@@ -21,11 +21,18 @@
 //    barrier inside a level; a level ends when every CTA has finished its scan
 //    slice and every queued task is done, which the last event detects and
 //    publishes by atomicMax on `levels_done`.
-//  * Every wait is bounded (spin_limit); on expiry the kernel records
+//  * Every wait is bounded in time (wait_us); on expiry the kernel records
 //    KC_ERR_TIMEOUT and returns instead of trapping.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
+
+// Loads of the read-only CSR.  A kernel that peels graphs whose memory may be
+// reused while it runs (the serve kernel) defines KC_LDG as __ldcg, so that no
+// stale line of an earlier graph can be served from the non-coherent L1 path.
+#ifndef KC_LDG
+#define KC_LDG(p) __ldg(p)
+#endif
 
 namespace kc {
 
@@ -89,11 +96,13 @@ struct PeelArgs {
     uint32_t shell_cap;
     uint32_t max_level;         // max degree: no vertex survives past it
     uint32_t epoch;             // 1..255, tags this run's task entries
-    uint32_t spin_limit;        // bounded waits
+    uint32_t wait_us;           // longest a warp waits for others before it gives up (KC_ERR_TIMEOUT)
     unsigned long long* trace;  // optional per-level timestamps (kTraceFields per level)
     uint32_t trace_cap;         // levels the trace buffer holds
     uint32_t* alive[2];         // optional alive-vertex lists (roundup(V,128) each); null = dense scans only
     uint32_t E;                 // arcs (= off[V])
+    uint32_t zero_tasks;        // 1: the participants clear the task queue during level 0
+                                // (for callers that cannot launch a memset while peeling)
 };
 
 // Per-level trace words: level start (CTA 0), CTA 0 arrival, level announced
@@ -124,6 +133,14 @@ __device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long l
 __device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned long long v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// Device wall clock (ns) for time-bounded waits: __nanosleep durations are only
+// hints (observed far below the request), so limits are in time, not polls.
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ int ld_err(const int* p) {
     int v;

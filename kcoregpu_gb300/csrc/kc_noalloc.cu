@@ -138,7 +138,7 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
     a.V = V;
     a.max_level = V;   // the max degree is below V; only a safety stop
     a.epoch = s.epoch;
-    a.spin_limit = 1u << 22;
+    a.wait_us = 2000000;   // 2 s
     a.E = n_arcs;
     a.alive[0] = reinterpret_cast<uint32_t*>(s.base + kOffAlive0);
     a.alive[1] = reinterpret_cast<uint32_t*>(s.base + kOffAlive1);

@@ -1,0 +1,676 @@
+// Device code of the persistent single-graph peel for sm_103a: every level of
+// the level-synchronous peel (src/ours.cc:117-160) in one cooperative launch,
+// with no host round trip and no grid barrier inside a level.  See
+// kc_device.cuh for the claim protocol.  Included by kc_peel.cu (the normal and
+// the bounds-checked kernel) and by kc_serve.cu (gangs of the serve kernel,
+// with KC_PEEL_NO_KERNEL and its own KC_VNS).
+#pragma once
+#include "kc_device.cuh"
+#include "kc_peel.cuh"
+
+#ifndef KC_VNS
+#ifdef KC_CHECKED
+#define KC_VNS checked_variant
+#else
+#define KC_VNS fast_variant
+#endif
+#endif
+
+namespace kc {
+namespace KC_VNS {   // the normal and the bounds-checked build link into one library
+
+// Bounds check at an access site of warp `w` (no-op unless built with KC_CHECKED).
+#define IN(idx, size, site) KC_IN(w.a.ctl, (idx), (size), (site), w.level)
+
+struct WarpBatch {
+    uint32_t start[kItemCap];     // first arc of each item
+    uint32_t pref[kItemCap + 1];  // lengths, then exclusive prefix
+    uint32_t nstart[kItemCap];    // cascade list (next batch)
+    uint32_t nlen[kItemCap];
+};
+
+struct CtaShared {
+    WarpBatch wb[kPeelWarps];
+    unsigned int arrive[4];
+    unsigned int peeled[4];
+    unsigned int minv[4];
+    unsigned int poll_lock;
+    unsigned int hint_level;
+    unsigned int hint_avail;
+    unsigned int hint_done;
+    int hint_err;
+};
+
+// Scan modes of a level.  Once few vertices remain, the scan reads a list of
+// the still-alive vertices instead of the whole state array; the list is
+// rebuilt (compacted) whenever it is more than half dead.
+enum ScanMode : uint32_t { kDense = 0, kDenseCompact = 1, kList = 2, kListCompact = 3 };
+
+struct Warp {
+    const PeelArgs& a;
+    WarpBatch& b;
+    CtaShared& sh;
+    LevelSlot* slot;
+    unsigned long long task_base;
+    uint32_t level;
+    uint32_t kk;       // level + kBias
+    uint32_t nitems;   // items staged in b.start / b.pref (lengths)
+    uint32_t nnext;    // cascade entries in b.nstart / b.nlen
+    uint32_t peeled;   // claims not yet published
+    uint32_t nwt;      // warps of all participants
+    uint32_t nparts;   // participating CTAs (the whole grid, or a gang of the serve kernel)
+    uint32_t mode;     // ScanMode of this level
+    uint32_t list_len; // entries in the current alive list
+    uint32_t list_cur; // which alive buffer is current
+    uint32_t it;       // level iteration (levels may be skipped, iterations are consecutive)
+    uint32_t minv;     // smallest survivor state this lane's scan saw
+};
+
+// Optional per-level trace (kc_graph_trace): kTraceFields words per level.
+__device__ __forceinline__ void trace(const PeelArgs& a, uint32_t level, int field, unsigned long long v) {
+    if (a.trace && level < a.trace_cap) a.trace[(size_t)level * kTraceFields + field] = v;
+}
+
+// Pushes the arc range [start, start+len) of every lane with `pred` to the
+// level's task queue, split into chunks of kChunk arcs.
+__device__ __noinline__ void push_tasks(Warp& w, bool pred, uint32_t start, uint32_t len) {
+    const unsigned lane = lane_id();
+    uint32_t nch = pred ? (len + kChunk - 1) / kChunk : 0;
+    uint32_t tot;
+    uint32_t ex = warp_excl_scan(nch, &tot);
+    if (tot == 0) return;
+    uint32_t base = 0;
+    if (lane == 0) {
+        base = atomicAdd(&w.slot->tail, tot);
+        atomicAdd(&w.a.ctl->tasks, (unsigned long long)tot);
+    }
+    base = __shfl_sync(kFull, base, 0);
+    const unsigned long long first = w.task_base + base;
+    if (first + tot > w.a.task_cap) {
+        if (lane == 0) record_error(w.a.ctl, kErrOverflow, w.level);
+        return;
+    }
+    unsigned m = __ballot_sync(kFull, nch != 0);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const uint32_t s0 = __shfl_sync(kFull, start, src);
+        const uint32_t l0 = __shfl_sync(kFull, len, src);
+        const uint32_t e0 = __shfl_sync(kFull, ex, src);
+        const uint32_t c0 = (l0 + kChunk - 1) / kChunk;
+        for (uint32_t c = lane; c < c0; c += 32) {
+            const uint32_t cs = s0 + c * kChunk;
+            const uint32_t cl = min(kChunk, l0 - c * kChunk);
+            if (IN(first + e0 + c, w.a.task_cap, 1))
+                st_relaxed64(&w.a.tasks[first + e0 + c], make_task(cs, cl, w.level, w.a.epoch));
+        }
+    }
+}
+
+// Handles the vertices claimed by this warp in one walk step: records the
+// core number (and peel order), then queues their adjacency on the cascade
+// list or, for hubs and list overflow, on the global task queue.
+__device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u) {
+    const unsigned m = __ballot_sync(kFull, found);
+    if (!m) return;
+    const unsigned lane = lane_id();
+    const uint32_t cnt = __popc(m);
+    w.peeled += cnt;
+    uint32_t start = 0, len = 0;
+    if (found && IN(u, w.a.V, 2)) {
+        w.a.core[u] = w.level;
+        start = KC_LDG(w.a.off + u);
+        len = KC_LDG(w.a.off + u + 1) - start;
+    }
+    if (w.a.order) {
+        uint32_t pos = 0;
+        if (lane == 0) pos = atomicAdd(&w.a.ctl->order_tail, cnt);
+        pos = __shfl_sync(kFull, pos, 0);
+        const uint32_t op = pos + __popc(m & lanemask_lt());
+        if (found && IN(op, w.a.V, 4)) w.a.order[op] = u;
+    }
+    bool local = found && len <= kLocalArcs;
+    unsigned lm = __ballot_sync(kFull, local);
+    if (w.nnext + __popc(lm) > kItemCap) { local = false; lm = 0; }
+    if (local) {
+        const uint32_t idx = w.nnext + __popc(lm & lanemask_lt());
+        if (!IN(idx, kItemCap, 24)) return;
+        w.b.nstart[idx] = start;
+        w.b.nlen[idx] = len;
+    }
+    w.nnext += __popc(lm);
+    const bool glob = found && !local;
+    if (__ballot_sync(kFull, glob)) push_tasks(w, glob, start, len);
+}
+
+// One neighbour u of a vertex peeled at this level (ours.cc:91-106): returns
+// true when this thread's decrement took u to the level and claimed it.
+__device__ __forceinline__ bool decrement(uint32_t* wp, uint32_t d, uint32_t kk) {
+    if (!(d > kk && d < kClaim)) return false;
+    const uint32_t old = atomicSub(wp, 1u);
+    if (old == kk + 1) return !(atomicOr(wp, kClaim) & kClaim);
+    if (old <= kk || old >= kClaim) atomicAdd(wp, 1u);   // undo (ours.cc:102-105)
+    return false;
+}
+
+// Walks every arc of the staged items (b.start / b.pref hold first arc and
+// length), lanes striding over the concatenated arcs (ours.cc:82-107); each
+// lane keeps four arcs in flight.
+__device__ void walk_items(Warp& w) {
+    const unsigned lane = lane_id();
+    const uint32_t n = w.nitems;
+    w.nitems = 0;
+    if (n == 0) return;
+    // lengths -> exclusive prefix, 4 items per lane
+    uint32_t l[4], s4 = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t i = lane * 4 + j;
+        l[j] = i < n ? w.b.pref[i] : 0;
+        s4 += l[j];
+    }
+    uint32_t total;
+    uint32_t ex = warp_excl_scan(s4, &total);
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t i = lane * 4 + j;
+        if (i < n) w.b.pref[i] = ex;
+        ex += l[j];
+    }
+    if (lane == 0) w.b.pref[n] = total;
+    __syncwarp();
+    const uint32_t kk = w.kk;
+    uint32_t lo = 0;
+    for (uint32_t base = 0; base < total; base += 128) {
+        uint32_t u[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t a = base + 32 * j + lane;
+            u[j] = 0xFFFFFFFFu;
+            if (a < total) {
+                uint32_t hi = n;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (w.b.pref[mid] <= a) lo = mid; else hi = mid;
+                }
+                const uint32_t arc = w.b.start[lo] + (a - w.b.pref[lo]);
+                if (IN(lo, kItemCap, 22) && IN(arc, w.a.E, 5)) {
+                    u[j] = KC_LDG(w.a.nbr + arc);
+                    if (!IN(u[j], w.a.V, 6)) u[j] = 0xFFFFFFFFu;
+                }
+            }
+        }
+        uint32_t d[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) d[j] = (u[j] != 0xFFFFFFFFu) ? __ldcg(w.a.w + u[j]) : 0u;
+        bool f[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) f[j] = (u[j] != 0xFFFFFFFFu) && decrement(w.a.w + u[j], d[j], kk);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) on_claimed(w, f[j], u[j]);
+    }
+    __syncwarp();
+}
+
+// Walks the staged items and then, while the cascade list is non-empty, the
+// vertices it discovered in the same level.
+__device__ void walk_with_cascades(Warp& w) {
+    walk_items(w);
+    const unsigned lane = lane_id();
+    while (w.nnext) {
+        const uint32_t n = w.nnext;
+        for (uint32_t i = lane; i < n; i += 32) {
+            w.b.start[i] = w.b.nstart[i];
+            w.b.pref[i] = w.b.nlen[i];
+        }
+        __syncwarp();
+        w.nnext = 0;
+        w.nitems = n;
+        walk_items(w);
+    }
+}
+
+// Stages the claimed vertices v[j] (mask bits, up to 4 per lane) as walk
+// items; hubs go to the task queue.  Flushes the batch first when it could
+// overflow.
+__device__ __forceinline__ void stage_claims(Warp& w, const uint32_t (&v)[4], unsigned mine) {
+    uint32_t st[4], ln[4];
+    unsigned localm = 0, hubm = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        st[j] = 0; ln[j] = 0;
+        if (mine & (1u << j)) {
+            if (!IN(v[j], w.a.V, 8)) continue;
+            st[j] = KC_LDG(w.a.off + v[j]);
+            ln[j] = KC_LDG(w.a.off + v[j] + 1) - st[j];
+            if (ln[j] == 0) continue;
+            if (ln[j] <= kLocalArcs) localm |= 1u << j; else hubm |= 1u << j;
+        }
+    }
+    const uint32_t cnt = __popc(localm);
+    uint32_t tot;
+    const uint32_t ex = warp_excl_scan(cnt, &tot);
+    if (tot && w.nitems + tot > kItemCap) walk_with_cascades(w);
+    uint32_t pos = w.nitems + ex;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if ((localm & (1u << j)) && IN(pos, kItemCap, 23)) { w.b.start[pos] = st[j]; w.b.pref[pos] = ln[j]; ++pos; }
+    w.nitems += tot;
+    __syncwarp();
+    if (__ballot_sync(kFull, hubm != 0)) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const bool h = (hubm >> j) & 1u;
+            if (__ballot_sync(kFull, h)) push_tasks(w, h, st[j], ln[j]);
+        }
+    }
+}
+
+// Appends this lane's survivors (mask bits of v[]) to the next alive list.
+__device__ __forceinline__ void append_survivors(Warp& w, const uint32_t (&v)[4], unsigned surv) {
+    const unsigned lane = lane_id();
+    uint32_t tot;
+    const uint32_t ex = warp_excl_scan(__popc(surv), &tot);
+    if (tot == 0) return;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&w.slot->alive_next, tot);
+    base = __shfl_sync(kFull, base, 0);
+    if (base + tot > w.a.V) {   // cannot happen: each vertex is appended once per level
+        if (lane == 0) record_error(w.a.ctl, kErrOverflow, w.level);
+        return;
+    }
+    base += ex;
+    uint32_t* out = w.a.alive[w.list_cur ^ 1u];
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if ((surv & (1u << j)) && IN(base, w.a.V, 9)) out[base++] = v[j];
+}
+
+// Claims (atomicOr) the hit vertices v[j]; returns the mask of those this
+// lane claimed, recording their core number.
+__device__ __forceinline__ unsigned claim_hits(Warp& w, const uint32_t (&v)[4], unsigned hit) {
+    unsigned o[4] = {kClaim, kClaim, kClaim, kClaim};
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if ((hit & (1u << j)) && IN(v[j], w.a.V, 10)) o[j] = atomicOr(w.a.w + v[j], kClaim);
+    unsigned mine = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+        if (!(o[j] & kClaim)) { mine |= 1u << j; w.a.core[v[j]] = w.level; }
+    return mine;
+}
+
+// Common tail of one scan step: publishes claims (peel order, count) and
+// stages their walk.
+__device__ __forceinline__ void after_claims(Warp& w, const uint32_t (&v)[4], unsigned mine) {
+    const unsigned lane = lane_id();
+    uint32_t tot;
+    const uint32_t ex = warp_excl_scan(__popc(mine), &tot);
+    if (tot == 0) return;
+    w.peeled += tot;
+    if (w.a.order) {
+        uint32_t pos = 0;
+        if (lane == 0) pos = atomicAdd(&w.a.ctl->order_tail, tot);
+        pos = __shfl_sync(kFull, pos, 0) + ex;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if ((mine & (1u << j)) && IN(pos, w.a.V, 12)) w.a.order[pos++] = v[j];
+    }
+    if (w.level > 0) stage_claims(w, v, mine);
+}
+
+// Scan of this warp's share of the vertices for level w.level (ours.cc:15-25):
+// either 128-vertex groups of the state array (uint4 loads) or 32-entry
+// groups of the alive list; every claimed vertex is walked inline.
+__device__ void scan_level(Warp& w, uint32_t gw) {
+    const unsigned lane = lane_id();
+    const PeelArgs& a = w.a;
+    const uint32_t kk = w.kk;
+    const bool compact = (w.mode == kDenseCompact || w.mode == kListCompact);
+    if (w.it == 0 && a.zero_tasks) {
+        // Level 0 pushes no task (its vertices have no arcs) and the next level
+        // starts only after every participant has arrived, so the queue can be
+        // cleared here instead of by a separate memset.
+        for (unsigned long long i = (unsigned long long)gw * 32 + lane; i < a.task_cap; i += (unsigned long long)w.nwt * 32)
+            a.tasks[i] = 0ull;
+    }
+    if (w.mode == kList || w.mode == kListCompact) {
+        const uint32_t* list = a.alive[w.list_cur];
+        const uint32_t n = w.list_len;
+        for (uint32_t i0 = gw * 32; i0 < n; i0 += w.nwt * 32) {
+            const uint32_t i = i0 + lane;
+            uint32_t v[4] = {0, 0, 0, 0};
+            uint32_t d = kClaim;
+            if (i < n && IN(i, a.V, 13)) {
+                v[0] = __ldcg(list + i);
+                if (v[0] < a.V) d = __ldcg(a.w + v[0]);
+                else record_error(a.ctl, kErrOverflow, w.level);   // defensive: never index past V
+            }
+            const unsigned hit = (d == kk) ? 1u : 0u;
+            const bool sv = d > kk && d < kClaim;
+            if (sv) w.minv = min(w.minv, d);
+            if (compact) append_survivors(w, v, sv ? 1u : 0u);
+            if (!__ballot_sync(kFull, hit != 0)) continue;
+            after_claims(w, v, claim_hits(w, v, hit));
+        }
+    } else {
+        const uint32_t ngroups = (a.V + 127) / 128;
+        uint4* w4 = reinterpret_cast<uint4*>(a.w);
+        for (uint32_t g = gw; g < ngroups; g += w.nwt) {
+            const uint32_t vb = g * 128 + lane * 4;
+            const uint32_t v[4] = {vb, vb + 1, vb + 2, vb + 3};
+            if (w.level == 0) {
+                // Level 0 also initialises the state from the offsets: isolated
+                // vertices are peeled here and have nothing to walk.
+                uint32_t st[4];
+                unsigned mine = 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (v[j] < a.V) {
+                        const uint32_t dg = KC_LDG(a.off + v[j] + 1) - KC_LDG(a.off + v[j]);
+                        if (dg == 0) { st[j] = kClaim | kBias; mine |= 1u << j; a.core[v[j]] = 0; }
+                        else st[j] = dg + kBias;
+                    } else {
+                        st[j] = kClaim | kBias;   // padding never matches
+                    }
+                }
+                if (IN(g * 32 + lane, (a.V + 127) / 128 * 32, 17))
+                    __stcg(w4 + g * 32 + lane, make_uint4(st[0], st[1], st[2], st[3]));
+                unsigned surv = 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (!(st[j] & kClaim)) { surv |= 1u << j; w.minv = min(w.minv, st[j]); }
+                if (compact) append_survivors(w, v, surv);
+                after_claims(w, v, mine);
+                continue;
+            }
+            const uint4 x = IN(g * 32 + lane, (a.V + 127) / 128 * 32, 18) ? __ldcg(w4 + g * 32 + lane)
+                                                                         : make_uint4(kClaim, kClaim, kClaim, kClaim);
+            const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+            unsigned hit = 0, surv = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (xs[j] == kk) hit |= 1u << j;
+                if (xs[j] > kk && xs[j] < kClaim) { surv |= 1u << j; w.minv = min(w.minv, xs[j]); }
+            }
+            if (compact) append_survivors(w, v, surv);
+            if (!__ballot_sync(kFull, hit != 0)) continue;
+            after_claims(w, v, claim_hits(w, v, hit));
+        }
+    }
+    walk_with_cascades(w);
+}
+
+// CTA-wide view of the level state: one warp at a time reads the global
+// counters (level completion, queue depth, error word) with independent
+// relaxed loads and leaves a hint in shared memory for the others, so idle
+// warps do not hammer one L2 line.  Returns 1 when the level is complete, -1
+// on a recorded error, else 0.
+__device__ __forceinline__ int level_state(Warp& w, uint32_t* avail) {
+    CtaShared& sh = w.sh;
+    const unsigned lane = lane_id();
+    unsigned done_v = 0, lvl = 0, av = 0;
+    int err = 0;
+    if (lane == 0) {
+        if (atomicCAS(&sh.poll_lock, 0u, 1u) == 0u) {
+            const unsigned ld = ld_relaxed(&w.a.ctl->iters_done);
+            const unsigned t = ld_relaxed(&w.slot->tail);
+            const unsigned h = ld_relaxed(&w.slot->head);
+            const int e = ld_err(&w.a.ctl->err);
+            *(volatile unsigned*)&sh.hint_done = ld;
+            *(volatile unsigned*)&sh.hint_avail = t > h ? t - h : 0u;
+            *(volatile unsigned*)&sh.hint_level = w.it;
+            *(volatile int*)&sh.hint_err = e;
+            __threadfence_block();
+            atomicExch(&sh.poll_lock, 0u);
+        }
+        done_v = *(volatile unsigned*)&sh.hint_done;
+        lvl = *(volatile unsigned*)&sh.hint_level;
+        av = *(volatile unsigned*)&sh.hint_avail;
+        err = *(volatile int*)&sh.hint_err;
+    }
+    done_v = __shfl_sync(kFull, done_v, 0);
+    lvl = __shfl_sync(kFull, lvl, 0);
+    av = __shfl_sync(kFull, av, 0);
+    err = __shfl_sync(kFull, err, 0);
+    *avail = (lvl == w.it) ? av : 0u;
+    if (done_v > w.it) return 1;
+    return err ? -1 : 0;
+}
+
+// Announces the level complete when every CTA has arrived and every task is
+// done.  Callers have just moved one of the counters behind a full fence and
+// read the other one with an ACQUIRE load, so the tail read below cannot be
+// performed before it: tail(t2) == done(t1) with t1 < t2 proves that no task
+// was in flight at t2 (both counters only grow and done <= tail).
+__device__ __forceinline__ void maybe_complete(Warp& w, unsigned arrivals, unsigned done) {
+    const unsigned t = ld_relaxed(&w.slot->tail);
+    if (arrivals == w.nparts && t == done) {
+        atomicMax(&w.a.ctl->iters_done, w.it + 1);
+        trace(w.a, w.it, 2, now_ns());
+    }
+}
+
+// Publishes `ndone` finished tasks.
+__device__ __forceinline__ void finish_tasks(Warp& w, uint32_t ndone) {
+    if (lane_id() == 0) {
+        fence_acq_rel();   // pushes and claims of these tasks before their completion
+        const unsigned long long add = ((unsigned long long)ndone << 32) | w.peeled;
+        const unsigned nd = (unsigned)((atomicAdd(&w.slot->done_peel, add) + add) >> 32);
+        __threadfence();
+        maybe_complete(w, (unsigned)(ld_acquire64(&w.slot->arr_peel) >> 32), nd);
+    }
+    w.peeled = 0;
+}
+
+// Claims and walks queued tasks until the level is complete.  Returns false
+// on error.
+__device__ bool drain_level(Warp& w) {
+    const unsigned lane = lane_id();
+    const PeelArgs& a = w.a;
+    unsigned pend = 0;
+    uint32_t cbase = 0;
+    unsigned long long waited_since = now_ns();
+    const unsigned long long limit_ns = (unsigned long long)a.wait_us * 1000ull;
+    uint32_t sleep_ns = 32;
+    for (;;) {
+        if (pend == 0) {
+            uint32_t avail;
+            const int ls = level_state(w, &avail);
+            if (ls > 0) return true;
+            if (ls < 0) return false;
+            if (avail) {
+                const uint32_t share = avail / max(1u, w.nwt / 2u);
+                const uint32_t B = min(32u, max(1u, share));
+                uint32_t c = 0;
+                if (lane == 0) c = atomicAdd(&w.slot->head, B);
+                cbase = __shfl_sync(kFull, c, 0);
+                pend = (B == 32) ? kFull : ((1u << B) - 1u);
+                waited_since = now_ns();
+                sleep_ns = 32;
+            } else {
+                if (now_ns() - waited_since > limit_ns) { if (lane == 0) record_error(a.ctl, kErrTimeout, w.level); return false; }
+                __nanosleep(sleep_ns);
+                sleep_ns = min(sleep_ns * 2, 128u);
+                continue;
+            }
+        }
+        bool ready = false;
+        unsigned long long e = 0;
+        if (pend & (1u << lane)) {
+            const unsigned long long pos = w.task_base + cbase + lane;
+            if (pos < a.task_cap) {
+                e = ld_relaxed64(&a.tasks[pos]);
+                ready = task_ready(e, w.level, a.epoch);
+            }
+        }
+        const unsigned rm = __ballot_sync(kFull, ready);
+        if (rm) {
+            if (ready) {
+                const uint32_t idx = __popc(rm & lanemask_lt());
+                w.b.start[idx] = (uint32_t)(e >> 32);
+                w.b.pref[idx] = (uint32_t)((e >> 24) & 0xFF) + 1u;
+            }
+            __syncwarp();
+            w.nitems = __popc(rm);
+            walk_with_cascades(w);
+            pend &= ~rm;
+            finish_tasks(w, __popc(rm));
+            waited_since = now_ns();
+            sleep_ns = 32;
+            continue;
+        }
+        uint32_t avail;
+        const int ls = level_state(w, &avail);
+        if (ls > 0) return true;   // claimed slots beyond the final tail
+        if (ls < 0) return false;
+        if (now_ns() - waited_since > limit_ns) { if (lane == 0) record_error(a.ctl, kErrTimeout, w.level); return false; }
+        __nanosleep(sleep_ns);
+        sleep_ns = min(sleep_ns * 2, 128u);
+    }
+}
+
+// The whole peel of one graph by `nparts` co-resident CTAs; this CTA is
+// participant `part`.  Every thread of the CTA calls it.  The persistent
+// kernel runs it with the whole grid; the serve kernel with a gang of CTAs.
+__device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint32_t nparts) {
+    const unsigned lane = lane_id();
+    const unsigned wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (threadIdx.x < 4) { sh.arrive[threadIdx.x] = 0; sh.peeled[threadIdx.x] = 0; sh.minv[threadIdx.x] = kFull; }
+    if (threadIdx.x == 0) { sh.poll_lock = 0; sh.hint_level = 0xFFFFFFFFu; sh.hint_avail = 0; sh.hint_done = 0; sh.hint_err = 0; }
+    __syncthreads();
+
+    Warp w{a, sh.wb[wid], sh, nullptr, 0ull, 0u, kBias, 0u, 0u, 0u, nparts * kPeelWarps, nparts, kDense, 0u, 0u,
+           0u, kFull};
+    const uint32_t gw = part * kPeelWarps + wid;
+    PeelCtl* ctl = a.ctl;
+    const bool lists = a.alive[0] != nullptr && a.alive[1] != nullptr;
+    const bool lead = part == 0 && threadIdx.x == 0;
+    if (lead && a.shells && a.shell_cap) a.shells[0] = 0;
+    uint32_t peeled_total = 0;
+
+    for (uint32_t level = 0, it = 0;; ++it) {
+        w.level = level;
+        w.it = it;
+        w.kk = level + kBias;
+        w.slot = &ctl->slot[it & 3];
+        w.minv = kFull;
+        if (lead) {
+            trace(a, it, 0, now_ns());
+            LevelSlot* r = &ctl->slot[(it + 2) & 3];
+            r->tail = 0; r->head = 0; r->done_peel = 0; r->arr_peel = 0;
+            r->alive_next = 0; r->min_next = kFull;
+            __threadfence();
+        }
+        scan_level(w, gw);
+
+        // CTA arrival.  Each warp releases its writes at CTA scope and counts
+        // itself in shared memory; the last warp of the CTA publishes the
+        // CTA's claims and smallest survivor with one GPU-scope fence and one
+        // 64-bit atomic, and the arrival that completes the level announces it.
+        const uint32_t wmin = __reduce_min_sync(kFull, w.minv);
+        if (lane == 0) {
+            const unsigned r = it & 3;
+            if (w.peeled) atomicAdd(&sh.peeled[r], w.peeled);
+            if (wmin != kFull) atomicMin(&sh.minv[r], wmin);
+            __threadfence_block();
+            const unsigned x = atomicAdd(&sh.arrive[r], 1u);
+            if (x == kPeelWarps - 1) {
+                __threadfence_block();
+                const unsigned p = atomicExch(&sh.peeled[r], 0u);
+                const unsigned m = atomicExch(&sh.minv[r], kFull);
+                atomicExch(&sh.arrive[r], 0u);
+                if (m != kFull) atomicMin(&w.slot->min_next, m);
+                __threadfence();
+                if (part == 0) trace(a, it, 1, now_ns());
+                const unsigned long long add = (1ull << 32) | p;
+                const unsigned ar = (unsigned)((atomicAdd(&w.slot->arr_peel, add) + add) >> 32);
+                if (ar == nparts) {
+                    trace(a, it, 5, now_ns());
+                    __threadfence();
+                    maybe_complete(w, ar, (unsigned)(ld_acquire64(&w.slot->done_peel) >> 32));
+                }
+            }
+        }
+        w.peeled = 0;
+        __syncwarp();
+
+        if (!drain_level(w)) return;
+        fence_acq_rel();
+
+        unsigned t = 0, an = 0, mn = 0, pi = 0;
+        if (lane == 0) {
+            t = ld_relaxed(&w.slot->tail);
+            an = ld_relaxed(&w.slot->alive_next);
+            mn = ld_relaxed(&w.slot->min_next);
+            pi = (unsigned)ld_relaxed64(&w.slot->arr_peel) + (unsigned)ld_relaxed64(&w.slot->done_peel);
+        }
+        t = __shfl_sync(kFull, t, 0);
+        an = __shfl_sync(kFull, an, 0);
+        mn = __shfl_sync(kFull, mn, 0);
+        pi = __shfl_sync(kFull, pi, 0);
+        w.task_base += t;
+        peeled_total += pi;
+        if (lead) {
+            trace(a, it, 3, now_ns());
+            trace(a, it, 4, peeled_total);
+            if (a.shells && level + 1 < a.shell_cap) a.shells[level + 1] = peeled_total;
+        }
+        if (peeled_total >= a.V) {
+            if (lead) { ctl->kmax = level; ctl->levels = level + 1; ctl->iterations = it + 1; }
+            return;
+        }
+        if (level >= a.max_level) {
+            if (lane == 0) record_error(ctl, kErrOverflow, level);
+            return;
+        }
+        // Next level.  A level that peeled nothing changed no degree, so every
+        // level below the smallest survivor state its scan saw is empty too and
+        // is skipped (its k-shell offset repeats).
+        uint32_t next = level + 1;
+        if (pi == 0 && mn != kFull && mn - kBias > next) next = mn - kBias;
+        if (lead && a.shells)
+            for (uint32_t l = level + 2; l <= next && l < a.shell_cap; ++l) a.shells[l] = peeled_total;
+        level = next;
+        // Scan mode of the next level (identical in every warp: it depends only
+        // on the peeled count and the list length, both final here).
+        if (w.mode == kDenseCompact || w.mode == kListCompact) {
+            w.list_cur ^= 1u;
+            w.list_len = min(an, a.V);
+        }
+        const uint32_t alive = a.V - peeled_total;
+        if (!lists) {
+            w.mode = kDense;
+        } else if (w.mode == kDense) {
+            w.mode = (alive <= a.V / 4) ? kDenseCompact : kDense;
+        } else {
+            w.mode = (alive <= w.list_len / 2) ? kListCompact : kList;
+        }
+    }
+}
+
+
+#ifndef KC_PEEL_NO_KERNEL
+#ifdef KC_CHECKED
+#define KC_PEEL_KERNEL peel_persistent_kernel_checked
+#define KC_PEEL_FN peel_persistent_fn_checked
+#else
+#define KC_PEEL_KERNEL peel_persistent_kernel
+#define KC_PEEL_FN peel_persistent_fn
+#endif
+
+__global__ void __launch_bounds__(kPeelThreads, 2) KC_PEEL_KERNEL(const __grid_constant__ PeelArgs a) {
+    __shared__ CtaShared sh;
+    peel_body(a, sh, blockIdx.x, gridDim.x);
+}
+#endif
+
+}  // namespace KC_VNS
+
+#ifndef KC_PEEL_NO_KERNEL
+const void* KC_PEEL_FN() { return reinterpret_cast<const void*>(&KC_VNS::KC_PEEL_KERNEL); }
+#endif
+
+}  // namespace kc

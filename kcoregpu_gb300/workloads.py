@@ -60,3 +60,37 @@ def batch_algorithmic_bytes(seg, kmax) -> int:
     k = np.asarray(kmax, dtype=np.int64)
     k = np.where(k == 0xFFFFFFFF, -1, k)
     return int((4 * (V + 1) + 4 * A + 4 * V * (k + 1)).sum())
+
+
+SERVED = dict(name="served-poisson-rmat-chunglu+rmat-s24", requests=240, seed_base=5000, mmin=10_000,
+              mmax=8_000_000, big_position=120, big_scale=24, big_edge_factor=16)
+
+
+def served_request(i: int, mmin: int | None = None, mmax: int | None = None):
+    """Request i of the served stream: m ~ log-uniform[10K, 8M] undirected edges,
+    alternating R-MAT (m draws, n = m/8 vertices) and Chung-Lu (gamma ~
+    U[2.1, 2.5], n = m/4, max weight sqrt(n)*8), seed 5000+i -> (offsets, neighbors)."""
+    import math
+    import numpy as np
+    c = SERVED
+    lo, hi = mmin or c["mmin"], mmax or c["mmax"]
+    rng = np.random.default_rng(c["seed_base"] + i)
+    m = int(math.exp(rng.uniform(math.log(lo), math.log(hi))))
+    seed = c["seed_base"] + i
+    if i % 2 == 0:
+        n = max(64, m // 8)
+        s, t = G.gen_rmat(n, m, seed)
+    else:
+        n = max(64, m // 4)
+        s, t = G.gen_chung_lu(n, m, float(rng.uniform(2.1, 2.5)), math.sqrt(n) * 8.0, seed)
+    off, nbr, _ = G.build_csr(s, t)
+    return off, nbr
+
+
+def served_big():
+    """The R-MAT scale-24 edge-factor-16 graph (2^24 vertices, 2^28 draws)."""
+    c = SERVED
+    n = 1 << c["big_scale"]
+    s, t = G.gen_rmat(n, n * c["big_edge_factor"], c["seed_base"] + 99999)
+    off, nbr, _ = G.build_csr(s, t)
+    return off, nbr
