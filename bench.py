@@ -236,12 +236,67 @@ def batched_leg(args, torch, flush, with_cpu: bool, with_baseline: bool = True):
     return out
 
 
+def served_leg(requests: int, mmax: int | None, with_big: bool, rates, seed: int = 5):
+    """Continuous batching: a seeded Poisson stream of requests submitted to the
+    server at each arrival rate (and all at once for saturation); latency is
+    submit -> core numbers on the host.  The plain one-graph-at-a-time peel
+    (kc_peel_csr per request, upload and download included) runs the same
+    stream for comparison."""
+    import kcoregpu_gb300 as kc
+    from kcoregpu_gb300 import workloads as W
+    from kcoregpu_gb300.serve import Server
+    t0 = time.perf_counter()
+    reqs = [W.served_request(i, mmax=mmax) for i in range(requests)]
+    big_pos = None
+    if with_big:
+        big_pos = requests // 2
+        reqs.insert(big_pos, W.served_big())
+    gen_s = time.perf_counter() - t0
+    edges = [len(n) // 2 for _, n in reqs]
+    srv = Server()
+    srv.wait(srv.submit(*reqs[0]))   # warm-up (kernel launch, pool growth)
+    rng = np.random.default_rng(seed)
+    sweep = []
+    for rate in list(rates) + [None]:
+        gaps = rng.exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
+        arrive = np.cumsum(gaps) - gaps[0]
+        ids = []
+        start = time.perf_counter()
+        for a, (o, n) in zip(arrive, reqs):
+            while time.perf_counter() - start < a:
+                time.sleep(min(0.0005, max(0.0, a - (time.perf_counter() - start))))
+            ids.append(srv.submit(o, n))
+        res = [srv.wait(r, timeout_s=300) for r in ids]
+        span = time.perf_counter() - start
+        lat = np.array([t["latency_us"] for _, _, t in res]) / 1e3
+        pt = {"rate": rate or "all-at-once", "graphs_per_s": len(reqs) / span, "edges_per_s": sum(edges) / span,
+              "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+              "max_gang": max(t["gang"] for _, _, t in res)}
+        if big_pos is not None:
+            pt["big_graph_latency_ms"] = float(lat[big_pos])
+        sweep.append(pt)
+    st = srv.stats()
+    srv.close()
+    t1 = time.perf_counter()
+    for o, n in reqs:
+        kc.peel_csr(o, n)
+    plain_s = time.perf_counter() - t1
+    sat = sweep[-1]
+    return {"workload": W.SERVED["name"] if with_big else f"served-{requests}-requests-m<= {mmax}",
+            "requests": len(reqs), "undirected_edges": int(sum(edges)), "generation_s": gen_s,
+            "sweep": sweep, "saturated_graphs_per_s": sat["graphs_per_s"],
+            "plain_one_at_a_time": {"graphs_per_s": len(reqs) / plain_s, "seconds": plain_s,
+                                    "speedup_of_served": sat["graphs_per_s"] / (len(reqs) / plain_s)},
+            "peak_device_bytes": st["peak_in_use"], "blocks": st["blocks"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4])
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
+    ap.add_argument("--no-serve", action="store_true", help="skip the served leg of the default run")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched leg of the default run")
@@ -265,6 +320,26 @@ def main():
     def barrier():
         if world > 1:
             torch.distributed.barrier()
+
+    if args.config == 5:
+        barrier()
+        with Clocks(local) as clk:
+            sv = served_leg(W_requests := 120, None, True, rates=[25, 50, 100, 200, 400, 800])
+        barrier()
+        if rank == 0:
+            sat = sv["sweep"][-1]
+            line = {"metric": METRIC, "value": world * sv["saturated_graphs_per_s"], "unit": "graphs/s",
+                    "n_gpus": world, "steps": W_requests, "warmup": 1, "ms_per_step": 1e3 / sv["saturated_graphs_per_s"],
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                    "data": "synthetic", "config": {"workload": sv["workload"], "requests": sv["requests"],
+                                                    "undirected_edges": sv["undirected_edges"],
+                                                    "inputs": "host memory, uploaded per request"},
+                    "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"],
+                    "e2e": {"value": world * sv["saturated_graphs_per_s"], "unit": "graphs/s",
+                            "note": "every request's upload and result download are inside its latency"},
+                    "clocks": clk.summary(), "served": sv}
+            print(json.dumps(line), flush=True)
+        return
 
     if args.config == 4:
         flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
@@ -413,6 +488,11 @@ def main():
             line["batched"] = bl
         except Exception as e:   # the single-graph line stands on its own
             line["batched"] = {"error": repr(e)[:200]}
+    if not args.no_serve:
+        try:   # a reduced sample of the served stream (the full one is --config 5)
+            line["served_sample"] = served_leg(60, 2_000_000, False, rates=[200, 800])
+        except Exception as e:
+            line["served_sample"] = {"error": repr(e)[:200]}
     print(json.dumps(line), flush=True)
 
 

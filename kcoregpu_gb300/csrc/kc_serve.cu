@@ -307,6 +307,18 @@ namespace {
 
 uint64_t align_up(uint64_t x) { return (x + 255) / 256 * 256; }
 
+// Host memcpy split over the host cores (one core alone copies far below the
+// host-device link rate).
+void parallel_copy(unsigned char* dst, const unsigned char* src, size_t n) {
+    if (n < (4u << 20)) { std::memcpy(dst, src, n); return; }
+    const int64_t parts = 16;
+#pragma omp parallel for schedule(static) num_threads(16)
+    for (int64_t i = 0; i < parts; ++i) {
+        const size_t a = n * (size_t)i / parts, b = n * (size_t)(i + 1) / parts;
+        std::memcpy(dst + a, src + a, b - a);
+    }
+}
+
 // Host -> device through the pinned staging halves, ordered on the copy stream.
 int stage_h2d(kc_server* s, void* dst, const void* src, size_t bytes) {
     const unsigned char* p = static_cast<const unsigned char*>(src);
@@ -315,7 +327,7 @@ int stage_h2d(kc_server* s, void* dst, const void* src, size_t bytes) {
         s->stage_next ^= 1;
         KC_CUDA(cudaEventSynchronize(s->stage_ev[k]));   // the half's previous copy has left
         const size_t n = std::min(bytes - done, s->stage_half);
-        std::memcpy(s->stage + k * s->stage_half, p + done, n);
+        parallel_copy(s->stage + k * s->stage_half, p + done, n);
         KC_CUDA(cudaMemcpyAsync(static_cast<unsigned char*>(dst) + done, s->stage + k * s->stage_half, n,
                                 cudaMemcpyHostToDevice, s->cs));
         KC_CUDA(cudaEventRecord(s->stage_ev[k], s->cs));
@@ -336,7 +348,7 @@ int stage_d2h(kc_server* s, void* dst, const void* src, size_t bytes) {
                                 cudaMemcpyDeviceToHost, s->cs));
         KC_CUDA(cudaEventRecord(s->stage_ev[k], s->cs));
         KC_CUDA(cudaEventSynchronize(s->stage_ev[k]));
-        std::memcpy(p + done, s->stage + k * s->stage_half, n);
+        parallel_copy(p + done, s->stage + k * s->stage_half, n);
         done += n;
     }
     return KC_OK;
