@@ -2,6 +2,7 @@
 // persistent cooperative launch, and the one-shot host-buffer entry point.
 // Replaces the reference's kcore() host loop (src/ours.cc:117-160) and its
 // device memory glue (src/gpu_memory_allocation.cu:4-22).
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -42,7 +43,11 @@ static bool checked_mode() {
 
 static const void* peel_kernel() { return checked_mode() ? peel_persistent_fn_checked() : peel_persistent_fn(); }
 
-// Persistent grid size per device: SMs x co-resident CTAs.
+// Persistent grid size per device: one CTA per SM (the kernel is compiled for
+// one 512-thread CTA per SM, up to 128 registers a thread).  The late levels
+// are short, and their cost grows with the participants that must arrive at
+// each level's end: on GB300 one CTA per SM was fastest (R-MAT 2^20: 3.7 ms at
+// 152 CTAs against 4.5 ms at 304, in a 64-register build that fit two).
 static int persistent_grid(int dev) {
     static std::mutex mu;
     static std::vector<int> cache;
@@ -53,12 +58,12 @@ static int persistent_grid(int dev) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_kernel(), kPeelThreads, 0);
     if (per < 1) per = 1;
-    cache[dev] = sms * per;
+    cache[dev] = sms;
     // KC_PEEL_GRID=n runs the persistent peel on n CTAs (n <= the co-resident
     // maximum): the level protocol is the one gangs of the serve kernel use.
     if (const char* e = std::getenv("KC_PEEL_GRID")) {
         const int n = std::atoi(e);
-        if (n > 0 && n < cache[dev]) cache[dev] = n;
+        if (n > 0 && n <= sms * per) cache[dev] = n;
     }
     return cache[dev];
 }
@@ -97,6 +102,15 @@ struct kc_graph {
     unsigned long long* d_trace = nullptr;
     uint32_t trace_cap = 0;
     uint32_t* d_alive[2] = {nullptr, nullptr};   // alive-vertex lists (scratch)
+    // tail hand-off (induced CSR of the survivors, local ids)
+    uint32_t tail_cap_v = 0;      // 0 = the persistent kernel peels every level
+    uint32_t tail_cap_arcs = 0;
+    uint32_t tail_items_cap = 0;
+    uint32_t* d_tail_ids = nullptr;
+    uint32_t* d_tail_off = nullptr;
+    uint32_t* d_tail_cur = nullptr;
+    uint32_t* d_tail_nbr = nullptr;
+    unsigned long long* d_tail_items = nullptr;
 };
 
 namespace {
@@ -109,6 +123,8 @@ void release(kc_graph* g) {
     cudaFree(g->d_order); cudaFree(g->d_shells); cudaFree(g->d_tasks); cudaFree(g->d_ctl);
     cudaFree(g->d_trace);
     cudaFree(g->d_alive[0]); cudaFree(g->d_alive[1]);
+    cudaFree(g->d_tail_ids); cudaFree(g->d_tail_off); cudaFree(g->d_tail_cur); cudaFree(g->d_tail_nbr);
+    cudaFree(g->d_tail_items);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     if (g->h_ctl_init) cudaFreeHost(g->h_ctl_init);
     if (g->ev0) cudaEventDestroy(g->ev0);
@@ -117,6 +133,66 @@ void release(kc_graph* g) {
 }
 
 uint64_t task_capacity(uint32_t V, uint64_t E) { return (uint64_t)V + E / kChunk + 64; }
+
+// Tail hand-off limits: at most KC_TAIL_V survivors (default and maximum
+// kTailV; 0 turns the hand-off off) whose induced arcs fit KC_TAIL_ARCS
+// (default kTailArcs).
+void tail_limits(uint32_t* cap_v, uint32_t* cap_arcs) {
+    static uint32_t v = 0, arcs = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        v = kTailV;
+        arcs = kTailArcs;
+        if (const char* e = std::getenv("KC_TAIL_V")) v = (uint32_t)std::min<long long>(std::max(0ll, std::atoll(e)), kTailV);
+        if (const char* e = std::getenv("KC_TAIL_ARCS"))
+            arcs = (uint32_t)std::min<long long>(std::max(1ll, std::atoll(e)), 1ll << 30);
+    });
+    *cap_v = v;
+    *cap_arcs = arcs;
+}
+
+// Buffers of the tail hand-off for a graph of at most E arcs.
+int reserve_tail(kc_graph* g, uint64_t E) {
+    uint32_t cap_v = 0, cap_arcs = 0;
+    tail_limits(&cap_v, &cap_arcs);
+    if (cap_v == 0) { g->tail_cap_v = 0; return KC_OK; }
+    // room for the padding of every adjacency to a multiple of 4 entries
+    cap_arcs = (uint32_t)(((std::min<uint64_t>(cap_arcs, std::max<uint64_t>(E, 1)) + 3ull * kTailV + 16) + 3) & ~3ull);
+    const uint64_t items = 2ull * cap_v + E / kFillChunk + 64;
+    if (items > 0xFFFFFFFFull) { g->tail_cap_v = 0; return KC_OK; }
+    if (!g->d_tail_ids) {
+        KC_CUDA(cudaMalloc(&g->d_tail_ids, sizeof(uint32_t) * kTailV));
+        KC_CUDA(cudaMalloc(&g->d_tail_off, sizeof(uint32_t) * (kTailV + 1)));
+        KC_CUDA(cudaMalloc(&g->d_tail_cur, sizeof(uint32_t) * kTailV));
+    }
+    if (cap_arcs > g->tail_cap_arcs || !g->d_tail_nbr) {
+        cudaFree(g->d_tail_nbr);
+        g->d_tail_nbr = nullptr;
+        KC_CUDA(cudaMalloc(&g->d_tail_nbr, sizeof(uint32_t) * cap_arcs));
+        g->tail_cap_arcs = cap_arcs;
+    }
+    if (items > g->tail_items_cap || !g->d_tail_items) {
+        cudaFree(g->d_tail_items);
+        g->d_tail_items = nullptr;
+        KC_CUDA(cudaMalloc(&g->d_tail_items, sizeof(unsigned long long) * items));
+        g->tail_items_cap = (uint32_t)items;
+    }
+    g->tail_cap_v = cap_v;
+    return KC_OK;
+}
+
+// The tail kernel with its shared-memory opt-in set on device `dev`.
+const void* tail_kernel(int dev) {
+    static std::mutex mu;
+    static std::vector<char> done;
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+    if (!done[dev]) {
+        cudaFuncSetAttribute(peel_tail_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)peel_tail_smem());
+        done[dev] = 1;
+    }
+    return peel_tail_fn();
+}
 
 // (Re)allocates device buffers for a graph of V vertices / E arcs.
 int reserve(kc_graph* g, uint32_t V, uint64_t E) {
@@ -148,7 +224,7 @@ int reserve(kc_graph* g, uint32_t V, uint64_t E) {
         g->task_cap = tc;
         g->epoch = 0;
     }
-    return KC_OK;
+    return reserve_tail(g, g->cap_E);
 }
 
 int graph_create(kc_graph** out) {
@@ -259,9 +335,22 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     a.alive[1] = g->d_alive[1];
     a.trace = with_trace ? g->d_trace : nullptr;
     a.trace_cap = with_trace ? g->trace_cap : 0;
+    const bool tail = g->tail_cap_v != 0;
+    if (tail) {
+        a.tail_cap_v = g->tail_cap_v;
+        a.tail_cap_arcs = g->tail_cap_arcs;
+        a.tail_ids = g->d_tail_ids;
+        a.tail_off = g->d_tail_off;
+        a.tail_cur = g->d_tail_cur;
+        a.tail_nbr = g->d_tail_nbr;
+        a.tail_items = g->d_tail_items;
+        a.tail_items_cap = g->tail_items_cap;
+    }
     void* args[] = {&a};
     KC_CUDA(cudaEventRecord(g->ev0, g->stream));
     KC_CUDA(cudaLaunchCooperativeKernel(peel_kernel(), dim3(g->grid), dim3(kPeelThreads), args, 0, g->stream));
+    if (tail)
+        KC_CUDA(cudaLaunchKernel(tail_kernel(g->dev), dim3(1), dim3(kTailThreads), args, peel_tail_smem(), g->stream));
     KC_CUDA(cudaEventRecord(g->ev1, g->stream));
     KC_CUDA(cudaMemcpyAsync(g->h_ctl, g->d_ctl, sizeof(PeelCtl), cudaMemcpyDeviceToHost, g->stream));
     g->pending = true;

@@ -231,7 +231,7 @@ int kc_batch_upload(const kc_segcsr* s, kc_batch** out) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_batch_fn(), kBatchThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gper, peel_persistent_fn(), kPeelThreads, 0);
-    b->ggrid = sms * std::max(1, gper);
+    b->ggrid = gper > 0 ? sms : 0;   // giants: one CTA per SM, as the single-graph peel
     autotune(b, sms, std::max(1, per));
     cudaError_t e;
 #define KC_B(call) do { e = (call); if (e != cudaSuccess) return fail(cuda_fail(e, #call)); } while (0)

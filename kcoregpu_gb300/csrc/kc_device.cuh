@@ -62,7 +62,8 @@ struct alignas(128) LevelSlot {
     unsigned int pad2[30];
     unsigned int alive_next;  // survivors appended to the next alive list
     unsigned int min_next;    // smallest survivor state seen by the scans (0xFFFFFFFF = none)
-    unsigned int pad3[30];
+    unsigned long long arcs_next;   // sum of the survivor degrees seen by the scans (>= induced arcs)
+    unsigned int pad3[28];
 };
 
 struct alignas(128) PeelCtl {
@@ -79,7 +80,15 @@ struct alignas(128) PeelCtl {
     unsigned int err_site;     // checked build: access site of the first violation
     unsigned int iterations;   // level iterations actually run (empty runs skipped)
     unsigned long long err_index;   // checked build: its index
-    unsigned int pad2[22];
+    unsigned int bar_count;    // grid barrier of the tail hand-off: arrivals
+    unsigned int bar_gen;      // and generation
+    unsigned int tail_n;       // vertices handed to the tail peel (0 = none)
+    unsigned int tail_level;   // first level of the tail peel
+    unsigned int tail_peeled;  // vertices peeled before it
+    unsigned int tail_iter;    // level iterations run before it
+    unsigned int tail_items;   // fill work items of the induced CSR
+    unsigned int tail_arcs;    // arcs of the induced CSR
+    unsigned int pad2[14];
 };
 
 struct PeelArgs {
@@ -103,7 +112,28 @@ struct PeelArgs {
     uint32_t E;                 // arcs (= off[V])
     uint32_t zero_tasks;        // 1: the participants clear the task queue during level 0
                                 // (for callers that cannot launch a memset while peeling)
+    // Tail hand-off (zero caps = never): once at most tail_cap_v vertices
+    // remain and their induced arcs fit tail_cap_arcs, the participants build
+    // the induced CSR of the survivors (local ids) and stop; peel_tail_kernel
+    // finishes the peel in one CTA with the states in shared memory.
+    uint32_t tail_cap_v = 0;
+    uint32_t tail_cap_arcs = 0;
+    uint32_t* tail_ids = nullptr;              // tail_cap_v: global id of each local vertex
+    uint32_t* tail_off = nullptr;              // tail_cap_v+1: induced CSR offsets
+    uint32_t* tail_cur = nullptr;              // tail_cap_v: fill cursors
+    uint32_t* tail_nbr = nullptr;              // tail_cap_arcs: induced CSR neighbours (local ids,
+                                               // each adjacency padded to 4 entries with 0xFFFFFFFF)
+    unsigned long long* tail_items = nullptr;  // fill work items: local id << 32 | arc chunk
+    uint32_t tail_items_cap = 0;
 };
+
+// Tail peel: one CTA of kTailThreads threads, states in shared memory.
+constexpr uint32_t kTailThreads = 1024;
+constexpr uint32_t kTailWarps = kTailThreads / 32;
+constexpr uint32_t kTailV = 16384;        // largest tail (shared-memory states)
+constexpr uint32_t kTailItems = 2048;     // queue entries walked per round
+constexpr uint32_t kTailArcs = 1u << 22;  // default largest induced CSR handed over
+constexpr uint32_t kFillChunk = 256;      // raw arcs per fill work item
 
 // Per-level trace words: level start (CTA 0), CTA 0 arrival, level announced
 // complete, CTA 0 saw completion, vertices peeled so far, last CTA arrival.

@@ -77,7 +77,7 @@ int noalloc_setup(int dev, DeviceScratch& s) {
         return KC_ERR_CUDA;
     }
     s.base = static_cast<unsigned char*>(p);
-    s.grid = sms * (per > 0 ? per : 1);
+    s.grid = sms;   // one CTA per SM, as the single-graph peel
     s.epoch = 0;
     s.ready = true;
     return KC_OK;

@@ -34,7 +34,9 @@ struct CtaShared {
     unsigned int arrive[4];
     unsigned int peeled[4];
     unsigned int minv[4];
+    unsigned long long arcs[4];
     unsigned int poll_lock;
+    int bar_ok;
     unsigned int hint_level;
     unsigned int hint_avail;
     unsigned int hint_done;
@@ -64,6 +66,7 @@ struct Warp {
     uint32_t list_cur; // which alive buffer is current
     uint32_t it;       // level iteration (levels may be skipped, iterations are consecutive)
     uint32_t minv;     // smallest survivor state this lane's scan saw
+    uint32_t arcs;     // sum of the survivor degrees this lane's scan saw (tail hand-off only)
 };
 
 // Optional per-level trace (kc_graph_trace): kTraceFields words per level.
@@ -349,7 +352,7 @@ __device__ void scan_level(Warp& w, uint32_t gw) {
             }
             const unsigned hit = (d == kk) ? 1u : 0u;
             const bool sv = d > kk && d < kClaim;
-            if (sv) w.minv = min(w.minv, d);
+            if (sv) { w.minv = min(w.minv, d); w.arcs += d - kBias; }
             if (compact) append_survivors(w, v, sv ? 1u : 0u);
             if (!__ballot_sync(kFull, hit != 0)) continue;
             after_claims(w, v, claim_hits(w, v, hit));
@@ -380,7 +383,7 @@ __device__ void scan_level(Warp& w, uint32_t gw) {
                 unsigned surv = 0;
 #pragma unroll
                 for (int j = 0; j < 4; ++j)
-                    if (!(st[j] & kClaim)) { surv |= 1u << j; w.minv = min(w.minv, st[j]); }
+                    if (!(st[j] & kClaim)) { surv |= 1u << j; w.minv = min(w.minv, st[j]); w.arcs += st[j] - kBias; }
                 if (compact) append_survivors(w, v, surv);
                 after_claims(w, v, mine);
                 continue;
@@ -392,7 +395,7 @@ __device__ void scan_level(Warp& w, uint32_t gw) {
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (xs[j] == kk) hit |= 1u << j;
-                if (xs[j] > kk && xs[j] < kClaim) { surv |= 1u << j; w.minv = min(w.minv, xs[j]); }
+                if (xs[j] > kk && xs[j] < kClaim) { surv |= 1u << j; w.minv = min(w.minv, xs[j]); w.arcs += xs[j] - kBias; }
             }
             if (compact) append_survivors(w, v, surv);
             if (!__ballot_sync(kFull, hit != 0)) continue;
@@ -531,6 +534,214 @@ __device__ bool drain_level(Warp& w) {
     }
 }
 
+// ------------------------------------------------------------ tail hand-off
+// Once few vertices remain, every later level touches a small induced
+// subgraph whose vertices still carry their full adjacency, and each level
+// costs the grid-wide arrival protocol.  The participants then build the
+// induced CSR of the survivors with local ids (their remaining degree is
+// their state, so the offsets need no count pass) and stop; peel_tail_kernel
+// finishes the peel in one CTA with the states in shared memory.
+
+// Barrier of the `nparts` co-resident participants, bounded in time.  Every
+// thread of the CTA calls it; false when the wait ran out or a participant
+// recorded an error.
+__device__ bool part_barrier(const PeelArgs& a, CtaShared& sh, uint32_t nparts, uint32_t level) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        PeelCtl* ctl = a.ctl;
+        int ok = 1;
+        const unsigned gen = ld_acquire(&ctl->bar_gen);
+        __threadfence();
+        if (atomicAdd(&ctl->bar_count, 1u) == nparts - 1) {
+            atomicExch(&ctl->bar_count, 0u);
+            __threadfence();
+            atomicAdd(&ctl->bar_gen, 1u);
+        } else {
+            const unsigned long long t0 = now_ns(), lim = (unsigned long long)a.wait_us * 1000ull;
+            while (ld_acquire(&ctl->bar_gen) == gen) {
+                if (ld_err(&ctl->err)) { ok = 0; break; }
+                if (now_ns() - t0 > lim) { record_error(ctl, kErrTimeout, level); ok = 0; break; }
+                __nanosleep(64);
+            }
+        }
+        if (ld_err(&ctl->err)) ok = 0;
+        sh.bar_ok = ok;
+    }
+    __syncthreads();
+    return sh.bar_ok != 0;
+}
+
+// Pass 1: every survivor (claim bit clear) gets a local id, its remaining
+// degree as the length of its induced adjacency, and fill work items of
+// kFillChunk raw arcs each.
+__device__ void tail_collect(Warp& w, uint32_t gw) {
+    const PeelArgs& a = w.a;
+    const unsigned lane = lane_id();
+    const uint32_t ngroups = (a.V + 127) / 128;
+    const uint4* w4 = reinterpret_cast<const uint4*>(a.w);
+    for (uint32_t g = gw; g < ngroups; g += w.nwt) {
+        const uint4 x = __ldcg(w4 + g * 32 + lane);
+        const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+        const uint32_t vb = g * 128 + lane * 4;
+        uint32_t nit[4], cnt = 0, items = 0;
+        unsigned alive = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            nit[j] = 0;
+            if (!(xs[j] & kClaim) && vb + j < a.V) {
+                alive |= 1u << j;
+                const uint32_t rd = KC_LDG(a.off + vb + j + 1) - KC_LDG(a.off + vb + j);
+                nit[j] = max(1u, (rd + kFillChunk - 1) / kFillChunk);
+                ++cnt;
+                items += nit[j];
+            }
+        }
+        if (!__ballot_sync(kFull, alive != 0)) continue;
+        uint32_t ctot, itot;
+        const uint32_t cex = warp_excl_scan(cnt, &ctot);
+        const uint32_t iex = warp_excl_scan(items, &itot);
+        uint32_t cb = 0, ib = 0;
+        if (lane == 0) {
+            cb = atomicAdd(&a.ctl->tail_n, ctot);
+            ib = atomicAdd(&a.ctl->tail_items, itot);
+        }
+        cb = __shfl_sync(kFull, cb, 0) + cex;
+        ib = __shfl_sync(kFull, ib, 0) + iex;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (!(alive & (1u << j))) continue;
+            if (cb < a.tail_cap_v && ib + nit[j] <= a.tail_items_cap) {
+                a.tail_ids[cb] = vb + j;
+                a.tail_off[cb + 1] = xs[j] - kBias;
+                for (uint32_t c = 0; c < nit[j]; ++c) a.tail_items[ib + c] = ((unsigned long long)cb << 32) | c;
+            } else {
+                record_error(a.ctl, kErrOverflow, w.level);
+            }
+            ++cb;
+            ib += nit[j];
+        }
+    }
+}
+
+// Pass 2: the state word of each survivor becomes its local id (claim bit
+// clear, so the fill pass tells survivors from peeled vertices by the same
+// bit), and CTA 0 turns the degrees into offsets and fill cursors.  Each
+// adjacency is padded to a multiple of 4 entries (pad = 0xFFFFFFFF) so that
+// the tail walk can read 16-byte quads; a cursor ends at offset + degree.
+__device__ void tail_offsets(Warp& w, CtaShared& sh, uint32_t gw, uint32_t part) {
+    const PeelArgs& a = w.a;
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    const uint32_t n = min(ld_relaxed(&a.ctl->tail_n), a.tail_cap_v);
+    for (uint32_t i = gw * 32 + lane; i < n; i += w.nwt * 32) {
+        const uint32_t v = __ldcg(a.tail_ids + i);
+        if (v < a.V) a.w[v] = i;
+    }
+    if (part != 0) return;
+    // Block-wide exclusive scan: thread t owns entries [t*per, (t+1)*per).
+    const uint32_t per = (n + kPeelThreads - 1) / kPeelThreads;
+    const uint32_t lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
+    uint32_t sum = 0;
+    for (uint32_t i = lo; i < hi; ++i) sum += (__ldcg(a.tail_off + i + 1) + 3u) & ~3u;
+    uint32_t wt;
+    const uint32_t ex = warp_excl_scan(sum, &wt);
+    uint32_t* tot = sh.wb[0].nstart;   // scratch: no walk is in flight
+    if (lane == 0) tot[wid] = wt;
+    __syncthreads();
+    if (wid == 0) {
+        const uint32_t t = lane < kPeelWarps ? tot[lane] : 0u;
+        uint32_t all;
+        const uint32_t te = warp_excl_scan(t, &all);
+        if (lane < kPeelWarps) tot[lane] = te;
+        if (lane == 0) {
+            tot[kPeelWarps] = all;
+            a.tail_off[0] = 0;
+            a.ctl->tail_arcs = all;
+            if (all > a.tail_cap_arcs) record_error(a.ctl, kErrOverflow, w.level);
+        }
+    }
+    __syncthreads();
+    uint32_t run = tot[wid] + ex;
+    const bool fits = tot[kPeelWarps] <= a.tail_cap_arcs;
+    for (uint32_t i = lo; i < hi; ++i) {
+        const uint32_t d = __ldcg(a.tail_off + i + 1);
+        const uint32_t pd = (d + 3u) & ~3u;
+        a.tail_cur[i] = run;
+        if (fits)
+            for (uint32_t p = run + d; p < run + pd; ++p) a.tail_nbr[p] = kFull;
+        run += pd;
+        a.tail_off[i + 1] = run;
+    }
+}
+
+// Pass 3: one fill item (kFillChunk raw arcs of one survivor) per warp; the
+// survivors among the neighbours are appended, as local ids, at the vertex's
+// fill cursor.  The order of a vertex's induced neighbours is immaterial.
+__device__ void tail_fill(Warp& w, uint32_t gw) {
+    const PeelArgs& a = w.a;
+    const unsigned lane = lane_id();
+    const uint32_t n = min(ld_relaxed(&a.ctl->tail_n), a.tail_cap_v);
+    const uint32_t ni = min(ld_relaxed(&a.ctl->tail_items), a.tail_items_cap);
+    constexpr int kPer = kFillChunk / 32;
+    for (uint32_t i = gw; i < ni; i += w.nwt) {
+        const unsigned long long item = __ldcg(a.tail_items + i);
+        const uint32_t lid = (uint32_t)(item >> 32), c = (uint32_t)item;
+        if (lid >= n) { if (lane == 0) record_error(a.ctl, kErrOverflow, w.level); continue; }
+        const uint32_t v = __ldcg(a.tail_ids + lid);
+        if (v >= a.V) { if (lane == 0) record_error(a.ctl, kErrOverflow, w.level); continue; }
+        const uint32_t s0 = KC_LDG(a.off + v) + c * kFillChunk;
+        const uint32_t e0 = min(s0 + kFillChunk, KC_LDG(a.off + v + 1));
+        uint32_t u[kPer];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t arc = s0 + j * 32 + lane;
+            u[j] = arc < e0 ? KC_LDG(a.nbr + arc) : kFull;
+        }
+        unsigned keep = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            if (u[j] < a.V) {
+                const uint32_t x = __ldcg(a.w + u[j]);
+                if (!(x & kClaim)) { keep |= 1u << j; u[j] = x; }
+            }
+        }
+        uint32_t tot;
+        const uint32_t ex = warp_excl_scan(__popc(keep), &tot);
+        if (tot == 0) continue;
+        uint32_t base = 0, end = 0;
+        if (lane == 0) {
+            base = atomicAdd(a.tail_cur + lid, tot);
+            end = __ldcg(a.tail_off + lid + 1);
+        }
+        base = __shfl_sync(kFull, base, 0);
+        end = __shfl_sync(kFull, end, 0);
+        if (base + tot > end || end > a.tail_cap_arcs) {   // a state disagrees with the adjacency
+            if (lane == 0) record_error(a.ctl, kErrOverflow, w.level);
+            continue;
+        }
+        uint32_t pos = base + ex;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j)
+            if (keep & (1u << j)) a.tail_nbr[pos++] = u[j];
+    }
+}
+
+// Builds the induced CSR of the survivors for the tail peel, which starts at
+// level `next` with `peeled_total` vertices peeled in `iters` iterations.
+__device__ void tail_handoff(Warp& w, CtaShared& sh, uint32_t gw, uint32_t part, uint32_t nparts, uint32_t next,
+                             uint32_t peeled_total, uint32_t iters) {
+    const PeelArgs& a = w.a;
+    if (part == 0 && threadIdx.x == 0) {
+        a.ctl->tail_level = next;
+        a.ctl->tail_peeled = peeled_total;
+        a.ctl->tail_iter = iters;
+    }
+    tail_collect(w, gw);
+    if (!part_barrier(a, sh, nparts, w.level)) return;
+    tail_offsets(w, sh, gw, part);
+    if (!part_barrier(a, sh, nparts, w.level)) return;
+    tail_fill(w, gw);
+}
+
 // The whole peel of one graph by `nparts` co-resident CTAs; this CTA is
 // participant `part`.  Every thread of the CTA calls it.  The persistent
 // kernel runs it with the whole grid; the serve kernel with a gang of CTAs.
@@ -538,12 +749,14 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
     const unsigned lane = lane_id();
     const unsigned wid = threadIdx.x >> 5;
     __syncthreads();
-    if (threadIdx.x < 4) { sh.arrive[threadIdx.x] = 0; sh.peeled[threadIdx.x] = 0; sh.minv[threadIdx.x] = kFull; }
+    if (threadIdx.x < 4) {
+        sh.arrive[threadIdx.x] = 0; sh.peeled[threadIdx.x] = 0; sh.minv[threadIdx.x] = kFull; sh.arcs[threadIdx.x] = 0;
+    }
     if (threadIdx.x == 0) { sh.poll_lock = 0; sh.hint_level = 0xFFFFFFFFu; sh.hint_avail = 0; sh.hint_done = 0; sh.hint_err = 0; }
     __syncthreads();
 
     Warp w{a, sh.wb[wid], sh, nullptr, 0ull, 0u, kBias, 0u, 0u, 0u, nparts * kPeelWarps, nparts, kDense, 0u, 0u,
-           0u, kFull};
+           0u, kFull, 0u};
     const uint32_t gw = part * kPeelWarps + wid;
     PeelCtl* ctl = a.ctl;
     const bool lists = a.alive[0] != nullptr && a.alive[1] != nullptr;
@@ -557,11 +770,12 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         w.kk = level + kBias;
         w.slot = &ctl->slot[it & 3];
         w.minv = kFull;
+        w.arcs = 0;
         if (lead) {
             trace(a, it, 0, now_ns());
             LevelSlot* r = &ctl->slot[(it + 2) & 3];
             r->tail = 0; r->head = 0; r->done_peel = 0; r->arr_peel = 0;
-            r->alive_next = 0; r->min_next = kFull;
+            r->alive_next = 0; r->min_next = kFull; r->arcs_next = 0;
             __threadfence();
         }
         scan_level(w, gw);
@@ -571,18 +785,22 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         // CTA's claims and smallest survivor with one GPU-scope fence and one
         // 64-bit atomic, and the arrival that completes the level announces it.
         const uint32_t wmin = __reduce_min_sync(kFull, w.minv);
+        const uint32_t warcs = __reduce_add_sync(kFull, w.arcs);
         if (lane == 0) {
             const unsigned r = it & 3;
             if (w.peeled) atomicAdd(&sh.peeled[r], w.peeled);
             if (wmin != kFull) atomicMin(&sh.minv[r], wmin);
+            if (warcs) atomicAdd(&sh.arcs[r], (unsigned long long)warcs);
             __threadfence_block();
             const unsigned x = atomicAdd(&sh.arrive[r], 1u);
             if (x == kPeelWarps - 1) {
                 __threadfence_block();
                 const unsigned p = atomicExch(&sh.peeled[r], 0u);
                 const unsigned m = atomicExch(&sh.minv[r], kFull);
+                const unsigned long long ca = atomicExch(&sh.arcs[r], 0ull);
                 atomicExch(&sh.arrive[r], 0u);
                 if (m != kFull) atomicMin(&w.slot->min_next, m);
+                if (ca) atomicAdd(&w.slot->arcs_next, ca);
                 __threadfence();
                 if (part == 0) trace(a, it, 1, now_ns());
                 const unsigned long long add = (1ull << 32) | p;
@@ -601,16 +819,19 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         fence_acq_rel();
 
         unsigned t = 0, an = 0, mn = 0, pi = 0;
+        unsigned long long ae = 0;
         if (lane == 0) {
             t = ld_relaxed(&w.slot->tail);
             an = ld_relaxed(&w.slot->alive_next);
             mn = ld_relaxed(&w.slot->min_next);
             pi = (unsigned)ld_relaxed64(&w.slot->arr_peel) + (unsigned)ld_relaxed64(&w.slot->done_peel);
+            ae = ld_relaxed64(&w.slot->arcs_next);
         }
         t = __shfl_sync(kFull, t, 0);
         an = __shfl_sync(kFull, an, 0);
         mn = __shfl_sync(kFull, mn, 0);
         pi = __shfl_sync(kFull, pi, 0);
+        ae = __shfl_sync(kFull, ae, 0);
         w.task_base += t;
         peeled_total += pi;
         if (lead) {
@@ -633,6 +854,14 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         if (pi == 0 && mn != kFull && mn - kBias > next) next = mn - kBias;
         if (lead && a.shells)
             for (uint32_t l = level + 2; l <= next && l < a.shell_cap; ++l) a.shells[l] = peeled_total;
+        // Hand the rest to the tail peel once it fits: few survivors, and the
+        // survivor degrees seen by this level's scans (an upper bound of the
+        // induced arcs) plus padding within the tail's CSR capacity.
+        if (a.tail_cap_v && a.V - peeled_total <= a.tail_cap_v &&
+            ae + 3ull * (a.V - peeled_total) <= a.tail_cap_arcs) {
+            tail_handoff(w, sh, gw, part, nparts, next, peeled_total, it + 1);
+            return;
+        }
         level = next;
         // Scan mode of the next level (identical in every warp: it depends only
         // on the peeled count and the list length, both final here).
@@ -661,7 +890,7 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
 #define KC_PEEL_FN peel_persistent_fn
 #endif
 
-__global__ void __launch_bounds__(kPeelThreads, 2) KC_PEEL_KERNEL(const __grid_constant__ PeelArgs a) {
+__global__ void __launch_bounds__(kPeelThreads, 1) KC_PEEL_KERNEL(const __grid_constant__ PeelArgs a) {
     __shared__ CtaShared sh;
     peel_body(a, sh, blockIdx.x, gridDim.x);
 }

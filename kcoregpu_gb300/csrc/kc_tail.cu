@@ -1,0 +1,225 @@
+// Tail of the single-graph peel for sm_103a: one CTA finishes the
+// level-synchronous peel (src/ours.cc:117-160) on the induced subgraph of the
+// survivors that the persistent kernel built when it stopped (local ids,
+// kc_peel_impl.cuh tail_handoff).  The states live in shared memory, so a
+// decrement is a shared-memory atomic and a level costs CTA barriers instead
+// of the grid-wide arrival protocol.  The walk follows the reference rule:
+// a neighbour whose degree is above the level is decremented, the decrement
+// that takes it to the level adds it to this level's queue, and a decrement
+// that raced below the level is undone (ours.cc:91-106).  Launched after the
+// persistent kernel on the same stream; it returns at once when no hand-off
+// happened.
+//
+// The induced CSR pads every adjacency to a multiple of 4 entries (pad =
+// 0xFFFFFFFF), so the walk reads 16-byte quads that never straddle two
+// vertices: each thread keeps kTailQuads quads (16 arcs) in flight.
+#include "kc_device.cuh"
+#include "kc_peel.cuh"
+
+namespace kc {
+namespace {
+
+constexpr int kTailQuads = 4;   // 16-byte quads per thread per walk step
+
+struct TailSmem {
+    uint32_t st[kTailV];              // remaining degree; the core number once peeled
+    uint32_t off[kTailV + 1];         // induced CSR offsets (multiples of 4)
+    uint32_t q[kTailV];               // local ids in peel order
+    uint32_t pref[kTailItems + 1];    // quad prefix of the items of one walk round
+    uint32_t start[kTailItems];       // first quad of each item
+    uint32_t warp_tot[kTailWarps];
+    uint32_t qtail;
+    uint32_t minv;
+    uint32_t total;
+};
+
+// Block-wide exclusive prefix sum of one value per thread.
+__device__ __forceinline__ uint32_t tail_scan(uint32_t x, TailSmem& s, uint32_t* total) {
+    const unsigned lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t wt;
+    const uint32_t ex = warp_excl_scan(x, &wt);
+    if (lane == 0) s.warp_tot[wid] = wt;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t all;
+        const uint32_t te = warp_excl_scan(s.warp_tot[lane], &all);
+        s.warp_tot[lane] = te;
+        if (lane == 0) s.total = all;
+    }
+    __syncthreads();
+    *total = s.total;
+    return s.warp_tot[wid] + ex;
+}
+
+// Appends the local ids v of the lanes with `pred` to the peel queue.
+__device__ __forceinline__ void tail_enqueue(TailSmem& s, bool pred, uint32_t v) {
+    const unsigned m = __ballot_sync(kFull, pred);
+    if (!m) return;
+    uint32_t pos = 0;
+    if ((threadIdx.x & 31) == 0) pos = atomicAdd(&s.qtail, (unsigned)__popc(m));
+    pos = __shfl_sync(kFull, pos, 0);
+    if (pred) {
+        const uint32_t p = pos + __popc(m & lanemask_lt());
+        if (p < kTailV) s.q[p] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid_constant__ PeelArgs a) {
+    extern __shared__ __align__(16) unsigned char tail_smem[];
+    TailSmem& s = *reinterpret_cast<TailSmem*>(tail_smem);
+    PeelCtl* ctl = a.ctl;
+    const unsigned tid = threadIdx.x, lane = tid & 31;
+    const uint32_t n = ctl->tail_n;
+    if (n == 0 || ctl->err != 0) return;
+    if (n > kTailV || n > a.tail_cap_v) {
+        if (tid == 0) record_error(ctl, kErrOverflow, ctl->tail_level);
+        return;
+    }
+    const uint32_t peeled0 = ctl->tail_peeled;
+    const uint32_t nquads = ctl->tail_arcs / 4;
+    const uint4* nbr4 = reinterpret_cast<const uint4*>(a.tail_nbr);
+    uint32_t level = ctl->tail_level;
+    uint32_t it = ctl->tail_iter;
+    for (uint32_t i = tid; i <= n; i += kTailThreads) s.off[i] = __ldcg(a.tail_off + i);
+    if (tid == 0) s.qtail = 0;
+    __syncthreads();
+    // the fill cursors stopped at offset + degree
+    for (uint32_t i = tid; i < n; i += kTailThreads) s.st[i] = __ldcg(a.tail_cur + i) - s.off[i];
+
+    bool failed = false;
+    for (;;) {
+        unsigned long long t_start = 0;
+        if (tid == 0) { s.minv = kFull; if (a.trace) t_start = now_ns(); }
+        __syncthreads();
+        const uint32_t lvl_start = s.qtail;
+        // scan: every vertex whose degree equals the level (ours.cc:15-25);
+        // peeled vertices keep the level they were peeled at, below this one
+        uint32_t mymin = kFull;
+        for (uint32_t b = 0; b < n; b += kTailThreads) {
+            const uint32_t v = b + tid;
+            const uint32_t d = v < n ? s.st[v] : 0u;
+            if (v < n && d > level) mymin = min(mymin, d);
+            tail_enqueue(s, v < n && d == level, v);
+        }
+        mymin = __reduce_min_sync(kFull, mymin);
+        if (lane == 0 && mymin != kFull) atomicMin(&s.minv, mymin);
+        __syncthreads();
+
+        // walk rounds over the queue, including the vertices the walk itself
+        // appends (same level)
+        uint32_t head = lvl_start, tail = min(s.qtail, n);   // each vertex is queued once
+        while (head < tail) {
+            const uint32_t m = min(tail - head, kTailItems);
+            const uint32_t i0 = 2 * tid, i1 = 2 * tid + 1;
+            uint32_t s0 = 0, s1 = 0, l0 = 0, l1 = 0;
+            if (i0 < m) { const uint32_t v = s.q[head + i0]; s0 = s.off[v] >> 2; l0 = (s.off[v + 1] >> 2) - s0; }
+            if (i1 < m) { const uint32_t v = s.q[head + i1]; s1 = s.off[v] >> 2; l1 = (s.off[v + 1] >> 2) - s1; }
+            uint32_t total;
+            const uint32_t ex = tail_scan(l0 + l1, s, &total);
+            if (i0 < m) { s.pref[i0] = ex; s.start[i0] = s0; }
+            if (i1 < m) { s.pref[i1] = ex + l0; s.start[i1] = s1; }
+            if (tid == 0) s.pref[m] = total;
+            __syncthreads();
+            uint32_t lo = 0;
+            for (uint32_t b = 0; b < total; b += kTailQuads * kTailThreads) {
+                uint4 x[kTailQuads];
+#pragma unroll
+                for (int j = 0; j < kTailQuads; ++j) {
+                    const uint32_t qi = b + j * kTailThreads + tid;
+                    x[j] = make_uint4(kFull, kFull, kFull, kFull);
+                    if (qi < total) {
+                        uint32_t hi = m;
+                        while (hi - lo > 1) {
+                            const uint32_t mid = (lo + hi) >> 1;
+                            if (s.pref[mid] <= qi) lo = mid; else hi = mid;
+                        }
+                        const uint32_t p = s.start[lo] + (qi - s.pref[lo]);
+                        if (p < nquads) x[j] = __ldcg(nbr4 + p);
+                    }
+                }
+                // decrements (ours.cc:91-106); pads and out-of-range ids are skipped
+                uint32_t hit = 0;
+#pragma unroll
+                for (int j = 0; j < kTailQuads; ++j) {
+                    const uint32_t u[4] = {x[j].x, x[j].y, x[j].z, x[j].w};
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        if (u[k] < n && s.st[u[k]] > level) {
+                            const uint32_t old = atomicSub(&s.st[u[k]], 1u);
+                            if (old == level + 1) hit |= 1u << (4 * j + k);
+                            else if (old <= level) atomicAdd(&s.st[u[k]], 1u);   // undo (ours.cc:102-105)
+                        }
+                    }
+                }
+                // the decrements that took a vertex to the level queue it
+                uint32_t htot;
+                const uint32_t hex = warp_excl_scan(__popc(hit), &htot);
+                if (htot) {
+                    uint32_t pos = 0;
+                    if (lane == 0) pos = atomicAdd(&s.qtail, htot);
+                    pos = __shfl_sync(kFull, pos, 0) + hex;
+#pragma unroll
+                    for (int j = 0; j < kTailQuads; ++j) {
+                        const uint32_t u[4] = {x[j].x, x[j].y, x[j].z, x[j].w};
+#pragma unroll
+                        for (int k = 0; k < 4; ++k)
+                            if ((hit >> (4 * j + k)) & 1u) { if (pos < kTailV) s.q[pos] = u[k]; ++pos; }
+                    }
+                }
+            }
+            __syncthreads();
+            head += m;
+            tail = min(s.qtail, n);
+        }
+        ++it;
+        const uint32_t peeled = peeled0 + tail;
+        if (tid == 0) {
+            if (a.trace && it - 1 < a.trace_cap) {
+                unsigned long long* row = a.trace + (size_t)(it - 1) * kTraceFields;
+                const unsigned long long t_end = now_ns();
+                row[0] = t_start; row[1] = t_end; row[2] = t_end; row[3] = t_end; row[4] = peeled; row[5] = t_end;
+            }
+            if (a.shells && level + 1 < a.shell_cap) a.shells[level + 1] = peeled;
+        }
+        if (tail >= n) break;
+        // A level that peeled nothing changed no degree: jump to the smallest
+        // survivor degree (every level in between is empty).
+        uint32_t next = level + 1;
+        const uint32_t mn = s.minv;
+        if (tail == lvl_start && mn != kFull && mn > next) next = mn;
+        if (next > a.max_level) {   // cannot happen for a valid CSR: every vertex is peeled by its degree
+            if (tid == 0) record_error(ctl, kErrOverflow, level);
+            failed = true;
+            break;
+        }
+        if (tid == 0 && a.shells)
+            for (uint32_t l = level + 2; l <= next && l < a.shell_cap; ++l) a.shells[l] = peeled;
+        level = next;
+        __syncthreads();   // every thread has read minv and qtail
+    }
+    if (failed) return;
+    // Outputs: the state of a peeled vertex is its core number; the queue is
+    // the peel order of the tail.
+    for (uint32_t i = tid; i < n; i += kTailThreads) {
+        const uint32_t v = __ldcg(a.tail_ids + i);
+        if (v < a.V) a.core[v] = s.st[i];
+    }
+    if (a.order) {
+        for (uint32_t p = tid; p < n; p += kTailThreads) {
+            const uint32_t lid = s.q[p];
+            if (lid < n && peeled0 + p < a.V) a.order[peeled0 + p] = __ldcg(a.tail_ids + lid);
+        }
+    }
+    if (tid == 0) {
+        ctl->kmax = level;
+        ctl->levels = level + 1;
+        ctl->iterations = it;
+    }
+}
+
+}  // namespace
+
+const void* peel_tail_fn() { return reinterpret_cast<const void*>(&peel_tail_kernel); }
+size_t peel_tail_smem() { return sizeof(TailSmem); }
+
+}  // namespace kc
