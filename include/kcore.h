@@ -142,10 +142,15 @@ int  kc_degeneracy_order(kc_graph* g, uint32_t* order_out,
                          uint32_t* shell_offsets_out, uint32_t shell_cap,
                          uint32_t* kmax);
 /* Tracing: runs a peel that records per-level device timestamps (ns of
- * %globaltimer) and counters, 6 words per level iteration: start, CTA 0
+ * %globaltimer) and counters, 8 words per level iteration: start, CTA 0
  * arrival, announced complete, CTA 0 saw completion, vertices peeled so far,
- * last CTA arrival.  out holds level_cap*6 words; *levels = iterations run.  (The
- * reference's per-level trace is a commented-out cout, src/ours.cc:148.)       */
+ * last CTA arrival, walk rounds, 16-byte adjacency quads walked.  Levels run by
+ * the one-CTA tail kernel have start, end (words 1, 2, 3, 5), peeled, rounds
+ * and quads; the first of them keeps the hand-off's times in words 1, 2, 5
+ * (both barriers passed, CTA 0's fill done) and starts at the tail kernel's
+ * entry; grid levels have 0 rounds and quads.  out holds level_cap*8 words;
+ * *levels = iterations run.  (The reference's per-level trace is a
+ * commented-out cout, src/ours.cc:148.)                                          */
 int  kc_graph_trace(kc_graph* g, uint64_t* out, uint32_t level_cap, uint32_t* levels);
 /* Device pointers of the resident CSR/core arrays (for zero-copy consumers).     */
 int  kc_graph_device_ptrs(kc_graph* g, const uint32_t** d_offsets,

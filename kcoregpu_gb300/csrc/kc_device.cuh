@@ -136,8 +136,9 @@ constexpr uint32_t kTailArcs = 1u << 22;  // default largest induced CSR handed 
 constexpr uint32_t kFillChunk = 256;      // raw arcs per fill work item
 
 // Per-level trace words: level start (CTA 0), CTA 0 arrival, level announced
-// complete, CTA 0 saw completion, vertices peeled so far, last CTA arrival.
-constexpr int kTraceFields = 6;
+// complete, CTA 0 saw completion, vertices peeled so far, last CTA arrival,
+// walk rounds and quads walked (tail kernel levels only).
+constexpr int kTraceFields = 8;
 
 // ---------------------------------------------------------------- memory ops
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {

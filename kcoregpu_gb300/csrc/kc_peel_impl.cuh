@@ -572,26 +572,41 @@ __device__ bool part_barrier(const PeelArgs& a, CtaShared& sh, uint32_t nparts, 
 }
 
 // Pass 1: every survivor (claim bit clear) gets a local id, its remaining
-// degree as the length of its induced adjacency, and fill work items of
-// kFillChunk raw arcs each.
-__device__ void tail_collect(Warp& w, uint32_t gw) {
+// degree as the length of its induced adjacency, and fill work items of at
+// most kFillChunk raw arcs (first arc << 32 | local id << 9 | length-1).  The
+// candidates are the current alive list when the scans keep one (a superset
+// of the survivors), else every vertex.
+__device__ void tail_collect(Warp& w, uint32_t gw, const uint32_t* list, uint32_t count) {
     const PeelArgs& a = w.a;
     const unsigned lane = lane_id();
-    const uint32_t ngroups = (a.V + 127) / 128;
-    const uint4* w4 = reinterpret_cast<const uint4*>(a.w);
-    for (uint32_t g = gw; g < ngroups; g += w.nwt) {
-        const uint4 x = __ldcg(w4 + g * 32 + lane);
-        const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
-        const uint32_t vb = g * 128 + lane * 4;
-        uint32_t nit[4], cnt = 0, items = 0;
+    const bool dense = list == nullptr;
+    const uint32_t nsteps = dense ? (a.V + 127) / 128 : (count + 127) / 128;
+    for (uint32_t g = gw; g < nsteps; g += w.nwt) {
+        uint32_t v[4], xs[4];
+        if (dense) {
+            const uint4 x = __ldcg(reinterpret_cast<const uint4*>(a.w) + g * 32 + lane);
+            xs[0] = x.x; xs[1] = x.y; xs[2] = x.z; xs[3] = x.w;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[j] = g * 128 + lane * 4 + j;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t i = g * 128 + j * 32 + lane;
+                v[j] = i < count ? __ldcg(list + i) : kFull;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) xs[j] = v[j] < a.V ? __ldcg(a.w + v[j]) : kClaim;
+        }
+        uint32_t st[4], rd[4], nit[4], cnt = 0, items = 0;
         unsigned alive = 0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            nit[j] = 0;
-            if (!(xs[j] & kClaim) && vb + j < a.V) {
+            st[j] = 0; rd[j] = 0; nit[j] = 0;
+            if (!(xs[j] & kClaim) && v[j] < a.V) {
                 alive |= 1u << j;
-                const uint32_t rd = KC_LDG(a.off + vb + j + 1) - KC_LDG(a.off + vb + j);
-                nit[j] = max(1u, (rd + kFillChunk - 1) / kFillChunk);
+                st[j] = KC_LDG(a.off + v[j]);
+                rd[j] = KC_LDG(a.off + v[j] + 1) - st[j];
+                nit[j] = (rd[j] + kFillChunk - 1) / kFillChunk;
                 ++cnt;
                 items += nit[j];
             }
@@ -611,9 +626,13 @@ __device__ void tail_collect(Warp& w, uint32_t gw) {
         for (int j = 0; j < 4; ++j) {
             if (!(alive & (1u << j))) continue;
             if (cb < a.tail_cap_v && ib + nit[j] <= a.tail_items_cap) {
-                a.tail_ids[cb] = vb + j;
+                a.tail_ids[cb] = v[j];
                 a.tail_off[cb + 1] = xs[j] - kBias;
-                for (uint32_t c = 0; c < nit[j]; ++c) a.tail_items[ib + c] = ((unsigned long long)cb << 32) | c;
+                for (uint32_t c = 0; c < nit[j]; ++c) {
+                    const uint32_t len = min(kFillChunk, rd[j] - c * kFillChunk);
+                    a.tail_items[ib + c] = ((unsigned long long)(st[j] + c * kFillChunk) << 32) |
+                                           ((unsigned long long)cb << 9) | (len - 1);
+                }
             } else {
                 record_error(a.ctl, kErrOverflow, w.level);
             }
@@ -625,10 +644,11 @@ __device__ void tail_collect(Warp& w, uint32_t gw) {
 
 // Pass 2: the state word of each survivor becomes its local id (claim bit
 // clear, so the fill pass tells survivors from peeled vertices by the same
-// bit), and CTA 0 turns the degrees into offsets and fill cursors.  Each
-// adjacency is padded to a multiple of 4 entries (pad = 0xFFFFFFFF) so that
-// the tail walk can read 16-byte quads; a cursor ends at offset + degree.
-__device__ void tail_offsets(Warp& w, CtaShared& sh, uint32_t gw, uint32_t part) {
+// bit), the induced CSR is preset to the pad value 0xFFFFFFFF up to its bound
+// (arcs_bound entries), and CTA 0 turns the degrees into offsets and fill
+// cursors.  Each adjacency is padded to a multiple of 4 entries so that the
+// tail walk can read 16-byte quads; a cursor ends at offset + degree.
+__device__ void tail_offsets(Warp& w, CtaShared& sh, uint32_t gw, uint32_t part, unsigned long long arcs_bound) {
     const PeelArgs& a = w.a;
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     const uint32_t n = min(ld_relaxed(&a.ctl->tail_n), a.tail_cap_v);
@@ -636,110 +656,152 @@ __device__ void tail_offsets(Warp& w, CtaShared& sh, uint32_t gw, uint32_t part)
         const uint32_t v = __ldcg(a.tail_ids + i);
         if (v < a.V) a.w[v] = i;
     }
+    const uint32_t nq = (uint32_t)(min(arcs_bound, (unsigned long long)a.tail_cap_arcs) / 4);
+    uint4* nbr4 = reinterpret_cast<uint4*>(a.tail_nbr);
+    for (uint32_t i = gw * 32 + lane; i < nq; i += w.nwt * 32) __stcg(nbr4 + i, make_uint4(kFull, kFull, kFull, kFull));
     if (part != 0) return;
-    // Block-wide exclusive scan: thread t owns entries [t*per, (t+1)*per).
-    const uint32_t per = (n + kPeelThreads - 1) / kPeelThreads;
-    const uint32_t lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
-    uint32_t sum = 0;
-    for (uint32_t i = lo; i < hi; ++i) sum += (__ldcg(a.tail_off + i + 1) + 3u) & ~3u;
-    uint32_t wt;
-    const uint32_t ex = warp_excl_scan(sum, &wt);
-    uint32_t* tot = sh.wb[0].nstart;   // scratch: no walk is in flight
-    if (lane == 0) tot[wid] = wt;
-    __syncthreads();
-    if (wid == 0) {
-        const uint32_t t = lane < kPeelWarps ? tot[lane] : 0u;
-        uint32_t all;
-        const uint32_t te = warp_excl_scan(t, &all);
-        if (lane < kPeelWarps) tot[lane] = te;
-        if (lane == 0) {
-            tot[kPeelWarps] = all;
-            a.tail_off[0] = 0;
-            a.ctl->tail_arcs = all;
-            if (all > a.tail_cap_arcs) record_error(a.ctl, kErrOverflow, w.level);
+    // Block-wide scan in tiles of kTile degrees staged in shared memory (the
+    // walk batches are free here): coalesced loads and stores, each thread
+    // scanning kTile/kPeelThreads consecutive entries of a tile.
+    constexpr uint32_t kTile = 4096;
+    constexpr uint32_t kPer = kTile / kPeelThreads;
+    static_assert(sizeof(sh.wb) >= sizeof(uint32_t) * (kTile + kPeelWarps + 1), "scan scratch");
+    uint32_t* buf = reinterpret_cast<uint32_t*>(&sh.wb[0]);
+    uint32_t* tot = buf + kTile;
+    uint32_t carry = 0;
+    for (uint32_t t0 = 0; t0 < n; t0 += kTile) {
+        const uint32_t m = min(kTile, n - t0);
+        uint32_t d[kPer];
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            const uint32_t i = threadIdx.x + k * kPeelThreads;
+            d[k] = i < m ? (__ldcg(a.tail_off + t0 + i + 1) + 3u) & ~3u : 0u;
         }
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) buf[threadIdx.x + k * kPeelThreads] = d[k];
+        __syncthreads();
+        uint32_t loc[kPer], sum = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) { loc[k] = buf[threadIdx.x * kPer + k]; sum += loc[k]; }
+        uint32_t wt;
+        const uint32_t ex = warp_excl_scan(sum, &wt);
+        if (lane == 0) tot[wid] = wt;
+        __syncthreads();
+        if (wid == 0) {
+            const uint32_t t = lane < kPeelWarps ? tot[lane] : 0u;
+            uint32_t all;
+            const uint32_t te = warp_excl_scan(t, &all);
+            if (lane < kPeelWarps) tot[lane] = te;
+            if (lane == 0) tot[kPeelWarps] = all;
+        }
+        __syncthreads();
+        uint32_t run = carry + tot[wid] + ex;
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) { run += loc[k]; buf[threadIdx.x * kPer + k] = run; }   // inclusive
+        __syncthreads();
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            const uint32_t i = threadIdx.x + k * kPeelThreads;
+            if (i < m) {
+                const uint32_t incl = buf[i];
+                a.tail_off[t0 + i + 1] = incl;
+                a.tail_cur[t0 + i] = incl - d[k];
+            }
+        }
+        carry += tot[kPeelWarps];
+        __syncthreads();
     }
-    __syncthreads();
-    uint32_t run = tot[wid] + ex;
-    const bool fits = tot[kPeelWarps] <= a.tail_cap_arcs;
-    for (uint32_t i = lo; i < hi; ++i) {
-        const uint32_t d = __ldcg(a.tail_off + i + 1);
-        const uint32_t pd = (d + 3u) & ~3u;
-        a.tail_cur[i] = run;
-        if (fits)
-            for (uint32_t p = run + d; p < run + pd; ++p) a.tail_nbr[p] = kFull;
-        run += pd;
-        a.tail_off[i + 1] = run;
+    if (threadIdx.x == 0) {
+        a.tail_off[0] = 0;
+        a.ctl->tail_arcs = carry;
+        if (carry > nq * 4u) record_error(a.ctl, kErrOverflow, w.level);   // beyond the preset bound
     }
 }
 
-// Pass 3: one fill item (kFillChunk raw arcs of one survivor) per warp; the
-// survivors among the neighbours are appended, as local ids, at the vertex's
-// fill cursor.  The order of a vertex's induced neighbours is immaterial.
+// Pass 3: fill items, kFillBatch per warp step; the survivors among an item's
+// neighbours are appended, as local ids, at the vertex's fill cursor.  The
+// order of a vertex's induced neighbours is immaterial.
 __device__ void tail_fill(Warp& w, uint32_t gw) {
     const PeelArgs& a = w.a;
     const unsigned lane = lane_id();
     const uint32_t n = min(ld_relaxed(&a.ctl->tail_n), a.tail_cap_v);
     const uint32_t ni = min(ld_relaxed(&a.ctl->tail_items), a.tail_items_cap);
     constexpr int kPer = kFillChunk / 32;
-    for (uint32_t i = gw; i < ni; i += w.nwt) {
-        const unsigned long long item = __ldcg(a.tail_items + i);
-        const uint32_t lid = (uint32_t)(item >> 32), c = (uint32_t)item;
-        if (lid >= n) { if (lane == 0) record_error(a.ctl, kErrOverflow, w.level); continue; }
-        const uint32_t v = __ldcg(a.tail_ids + lid);
-        if (v >= a.V) { if (lane == 0) record_error(a.ctl, kErrOverflow, w.level); continue; }
-        const uint32_t s0 = KC_LDG(a.off + v) + c * kFillChunk;
-        const uint32_t e0 = min(s0 + kFillChunk, KC_LDG(a.off + v + 1));
-        uint32_t u[kPer];
+    constexpr int kFillBatch = 4;
+    for (uint32_t i0 = gw; i0 < ni; i0 += kFillBatch * w.nwt) {
+        uint32_t lid[kFillBatch], u[kFillBatch][kPer];
 #pragma unroll
-        for (int j = 0; j < kPer; ++j) {
-            const uint32_t arc = s0 + j * 32 + lane;
-            u[j] = arc < e0 ? KC_LDG(a.nbr + arc) : kFull;
-        }
-        unsigned keep = 0;
+        for (int r = 0; r < kFillBatch; ++r) {
+            const uint32_t i = i0 + r * w.nwt;
+            const unsigned long long item = i < ni ? __ldcg(a.tail_items + i) : 0ull;
+            const uint32_t s0 = (uint32_t)(item >> 32);
+            const uint32_t len = i < ni ? ((uint32_t)item & 0x1FFu) + 1u : 0u;
+            lid[r] = i < ni ? ((uint32_t)item >> 9) : kFull;
 #pragma unroll
-        for (int j = 0; j < kPer; ++j) {
-            if (u[j] < a.V) {
-                const uint32_t x = __ldcg(a.w + u[j]);
-                if (!(x & kClaim)) { keep |= 1u << j; u[j] = x; }
+            for (int j = 0; j < kPer; ++j) {
+                const uint32_t k = j * 32 + lane;
+                u[r][j] = (k < len && s0 + k < a.E) ? KC_LDG(a.nbr + s0 + k) : kFull;
             }
         }
-        uint32_t tot;
-        const uint32_t ex = warp_excl_scan(__popc(keep), &tot);
-        if (tot == 0) continue;
-        uint32_t base = 0, end = 0;
-        if (lane == 0) {
-            base = atomicAdd(a.tail_cur + lid, tot);
-            end = __ldcg(a.tail_off + lid + 1);
-        }
-        base = __shfl_sync(kFull, base, 0);
-        end = __shfl_sync(kFull, end, 0);
-        if (base + tot > end || end > a.tail_cap_arcs) {   // a state disagrees with the adjacency
-            if (lane == 0) record_error(a.ctl, kErrOverflow, w.level);
-            continue;
-        }
-        uint32_t pos = base + ex;
+        unsigned keep[kFillBatch] = {};
 #pragma unroll
-        for (int j = 0; j < kPer; ++j)
-            if (keep & (1u << j)) a.tail_nbr[pos++] = u[j];
+        for (int r = 0; r < kFillBatch; ++r) {
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                if (u[r][j] < a.V) {
+                    const uint32_t x = __ldcg(a.w + u[r][j]);
+                    if (!(x & kClaim)) { keep[r] |= 1u << j; u[r][j] = x; }
+                }
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < kFillBatch; ++r) {
+            uint32_t tot;
+            const uint32_t ex = warp_excl_scan(__popc(keep[r]), &tot);
+            if (tot == 0) continue;
+            if (lid[r] >= n) { if (lane == 0) record_error(a.ctl, kErrOverflow, w.level); continue; }
+            uint32_t base = 0, end = 0;
+            if (lane == 0) {
+                base = atomicAdd(a.tail_cur + lid[r], tot);
+                end = __ldcg(a.tail_off + lid[r] + 1);
+            }
+            base = __shfl_sync(kFull, base, 0);
+            end = __shfl_sync(kFull, end, 0);
+            if (base + tot > end || end > a.tail_cap_arcs) {   // a state disagrees with the adjacency
+                if (lane == 0) record_error(a.ctl, kErrOverflow, w.level);
+                continue;
+            }
+            uint32_t pos = base + ex;
+#pragma unroll
+            for (int j = 0; j < kPer; ++j)
+                if (keep[r] & (1u << j)) a.tail_nbr[pos++] = u[r][j];
+        }
     }
 }
 
 // Builds the induced CSR of the survivors for the tail peel, which starts at
 // level `next` with `peeled_total` vertices peeled in `iters` iterations.
 __device__ void tail_handoff(Warp& w, CtaShared& sh, uint32_t gw, uint32_t part, uint32_t nparts, uint32_t next,
-                             uint32_t peeled_total, uint32_t iters) {
+                             uint32_t peeled_total, uint32_t iters, const uint32_t* list, uint32_t count,
+                             unsigned long long arcs_bound) {
     const PeelArgs& a = w.a;
     if (part == 0 && threadIdx.x == 0) {
         a.ctl->tail_level = next;
         a.ctl->tail_peeled = peeled_total;
         a.ctl->tail_iter = iters;
     }
-    tail_collect(w, gw);
+    // trace of the hand-off in the first tail row: fields 1, 2 and 5 = the
+    // two barriers passed and CTA 0's fill done
+    const bool lead = part == 0 && threadIdx.x == 0;
+    tail_collect(w, gw, list, count);
     if (!part_barrier(a, sh, nparts, w.level)) return;
-    tail_offsets(w, sh, gw, part);
+    if (lead) trace(a, iters, 1, now_ns());
+    tail_offsets(w, sh, gw, part, arcs_bound);
     if (!part_barrier(a, sh, nparts, w.level)) return;
+    if (lead) trace(a, iters, 2, now_ns());
     tail_fill(w, gw);
+    __syncthreads();
+    if (lead) trace(a, iters, 5, now_ns());
 }
 
 // The whole peel of one graph by `nparts` co-resident CTAs; this CTA is
@@ -859,7 +921,12 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         // induced arcs) plus padding within the tail's CSR capacity.
         if (a.tail_cap_v && a.V - peeled_total <= a.tail_cap_v &&
             ae + 3ull * (a.V - peeled_total) <= a.tail_cap_arcs) {
-            tail_handoff(w, sh, gw, part, nparts, next, peeled_total, it + 1);
+            // candidates: the list this level's scans appended to, or read
+            const bool appended = w.mode == kDenseCompact || w.mode == kListCompact;
+            const uint32_t* list = appended ? a.alive[w.list_cur ^ 1u] : (w.mode == kList ? a.alive[w.list_cur] : nullptr);
+            const uint32_t count = appended ? min(an, a.V) : w.list_len;
+            tail_handoff(w, sh, gw, part, nparts, next, peeled_total, it + 1, lists ? list : nullptr, count,
+                         (ae + 3ull * (a.V - peeled_total) + 3ull) & ~3ull);
             return;
         }
         level = next;

@@ -51,7 +51,8 @@ __device__ __forceinline__ uint32_t tail_scan(uint32_t x, TailSmem& s, uint32_t*
     return s.warp_tot[wid] + ex;
 }
 
-// Appends the local ids v of the lanes with `pred` to the peel queue.
+// Appends the local ids v of the lanes with `pred` to the peel queue; every
+// lane of the warp calls it.
 __device__ __forceinline__ void tail_enqueue(TailSmem& s, bool pred, uint32_t v) {
     const unsigned m = __ballot_sync(kFull, pred);
     if (!m) return;
@@ -80,11 +81,24 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
     const uint4* nbr4 = reinterpret_cast<const uint4*>(a.tail_nbr);
     uint32_t level = ctl->tail_level;
     uint32_t it = ctl->tail_iter;
-    for (uint32_t i = tid; i <= n; i += kTailThreads) s.off[i] = __ldcg(a.tail_off + i);
-    if (tid == 0) s.qtail = 0;
-    __syncthreads();
-    // the fill cursors stopped at offset + degree
-    for (uint32_t i = tid; i < n; i += kTailThreads) s.st[i] = __ldcg(a.tail_cur + i) - s.off[i];
+    const uint32_t it0 = it;
+    const unsigned long long t_entry = now_ns();
+    {   // offsets, and degrees from the fill cursors (they stopped at offset + degree)
+        constexpr uint32_t kPer = kTailV / kTailThreads;
+        uint32_t o[kPer], c[kPer];
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            const uint32_t i = tid + k * kTailThreads;
+            o[k] = i < n ? __ldcg(a.tail_off + i) : 0u;
+            c[k] = i < n ? __ldcg(a.tail_cur + i) : 0u;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kPer; ++k) {
+            const uint32_t i = tid + k * kTailThreads;
+            if (i < n) { s.off[i] = o[k]; s.st[i] = c[k] - o[k]; }
+        }
+        if (tid == 0) { s.off[n] = __ldcg(a.tail_off + n); s.qtail = 0; }
+    }
 
     bool failed = false;
     for (;;) {
@@ -95,11 +109,21 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         // scan: every vertex whose degree equals the level (ours.cc:15-25);
         // peeled vertices keep the level they were peeled at, below this one
         uint32_t mymin = kFull;
-        for (uint32_t b = 0; b < n; b += kTailThreads) {
-            const uint32_t v = b + tid;
-            const uint32_t d = v < n ? s.st[v] : 0u;
-            if (v < n && d > level) mymin = min(mymin, d);
-            tail_enqueue(s, v < n && d == level, v);
+        // 16-byte reads of 4 states; the loop bound is warp-uniform
+        for (uint32_t b0 = (tid >> 5) * 128; b0 < n; b0 += 4 * kTailThreads) {
+            const uint32_t b = b0 + 4 * lane;
+            const uint4 x = b < n ? *reinterpret_cast<const uint4*>(s.st + b) : make_uint4(0, 0, 0, 0);
+            const uint32_t d[4] = {x.x, x.y, x.z, x.w};
+            unsigned hit = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (b + k < n && d[k] > level) mymin = min(mymin, d[k]);
+                if (b + k < n && d[k] == level) hit |= 1u << k;
+            }
+            if (__any_sync(kFull, hit != 0)) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) tail_enqueue(s, (hit >> k) & 1u, b + k);
+            }
         }
         mymin = __reduce_min_sync(kFull, mymin);
         if (lane == 0 && mymin != kFull) atomicMin(&s.minv, mymin);
@@ -108,20 +132,42 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         // walk rounds over the queue, including the vertices the walk itself
         // appends (same level)
         uint32_t head = lvl_start, tail = min(s.qtail, n);   // each vertex is queued once
+        uint32_t rounds = 0, quads = 0;
         while (head < tail) {
+            ++rounds;
             const uint32_t m = min(tail - head, kTailItems);
             const uint32_t i0 = 2 * tid, i1 = 2 * tid + 1;
-            uint32_t s0 = 0, s1 = 0, l0 = 0, l1 = 0;
-            if (i0 < m) { const uint32_t v = s.q[head + i0]; s0 = s.off[v] >> 2; l0 = (s.off[v + 1] >> 2) - s0; }
-            if (i1 < m) { const uint32_t v = s.q[head + i1]; s1 = s.off[v] >> 2; l1 = (s.off[v + 1] >> 2) - s1; }
             uint32_t total;
-            const uint32_t ex = tail_scan(l0 + l1, s, &total);
-            if (i0 < m) { s.pref[i0] = ex; s.start[i0] = s0; }
-            if (i1 < m) { s.pref[i1] = ex + l0; s.start[i1] = s1; }
-            if (tid == 0) s.pref[m] = total;
-            __syncthreads();
+            if (m <= 64) {   // one warp holds every item: a warp scan and one barrier
+                if (tid < 32) {
+                    uint32_t s0 = 0, s1 = 0, l0 = 0, l1 = 0;
+                    if (i0 < m) { const uint32_t v = s.q[head + i0]; s0 = s.off[v] >> 2; l0 = (s.off[v + 1] >> 2) - s0; }
+                    if (i1 < m) { const uint32_t v = s.q[head + i1]; s1 = s.off[v] >> 2; l1 = (s.off[v + 1] >> 2) - s1; }
+                    uint32_t wt;
+                    const uint32_t ex = warp_excl_scan(l0 + l1, &wt);
+                    if (i0 < m) { s.pref[i0] = ex; s.start[i0] = s0; }
+                    if (i1 < m) { s.pref[i1] = ex + l0; s.start[i1] = s1; }
+                    if (tid == 0) { s.pref[m] = wt; s.total = wt; }
+                }
+                __syncthreads();
+                total = s.total;
+            } else {
+                uint32_t s0 = 0, s1 = 0, l0 = 0, l1 = 0;
+                if (i0 < m) { const uint32_t v = s.q[head + i0]; s0 = s.off[v] >> 2; l0 = (s.off[v + 1] >> 2) - s0; }
+                if (i1 < m) { const uint32_t v = s.q[head + i1]; s1 = s.off[v] >> 2; l1 = (s.off[v + 1] >> 2) - s1; }
+                const uint32_t ex = tail_scan(l0 + l1, s, &total);
+                if (i0 < m) { s.pref[i0] = ex; s.start[i0] = s0; }
+                if (i1 < m) { s.pref[i1] = ex + l0; s.start[i1] = s1; }
+                if (tid == 0) s.pref[m] = total;
+                __syncthreads();
+            }
+            // Quads are spread over all threads (thread t takes quads b + j *
+            // kTailThreads + t) so that a small round costs one quad per
+            // thread; warps past the round's end skip with a uniform branch.
+            const uint32_t wq = (tid & ~31u);   // this warp's first quad offset
             uint32_t lo = 0;
             for (uint32_t b = 0; b < total; b += kTailQuads * kTailThreads) {
+                if (b + wq >= total) break;   // warp-uniform
                 uint4 x[kTailQuads];
 #pragma unroll
                 for (int j = 0; j < kTailQuads; ++j) {
@@ -137,24 +183,31 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
                         if (p < nquads) x[j] = __ldcg(nbr4 + p);
                     }
                 }
-                // decrements (ours.cc:91-106); pads and out-of-range ids are skipped
+                // decrements (ours.cc:91-106); pads and out-of-range ids are
+                // skipped.  The degree pre-checks are read first: they only
+                // filter, the atomic's result decides.
                 uint32_t hit = 0;
 #pragma unroll
                 for (int j = 0; j < kTailQuads; ++j) {
+                    if (b + j * kTailThreads + wq >= total) break;   // warp-uniform
                     const uint32_t u[4] = {x[j].x, x[j].y, x[j].z, x[j].w};
+                    uint32_t d[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) d[k] = u[k] < n ? s.st[u[k]] : 0u;
+                    uint32_t old[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) old[k] = d[k] > level ? atomicSub(&s.st[u[k]], 1u) : 0u;
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
-                        if (u[k] < n && s.st[u[k]] > level) {
-                            const uint32_t old = atomicSub(&s.st[u[k]], 1u);
-                            if (old == level + 1) hit |= 1u << (4 * j + k);
-                            else if (old <= level) atomicAdd(&s.st[u[k]], 1u);   // undo (ours.cc:102-105)
-                        }
+                        if (d[k] <= level) continue;
+                        if (old[k] == level + 1) hit |= 1u << (4 * j + k);
+                        else if (old[k] <= level) atomicAdd(&s.st[u[k]], 1u);   // undo (ours.cc:102-105)
                     }
                 }
                 // the decrements that took a vertex to the level queue it
-                uint32_t htot;
-                const uint32_t hex = warp_excl_scan(__popc(hit), &htot);
-                if (htot) {
+                if (__any_sync(kFull, hit != 0)) {
+                    uint32_t htot;
+                    const uint32_t hex = warp_excl_scan(__popc(hit), &htot);
                     uint32_t pos = 0;
                     if (lane == 0) pos = atomicAdd(&s.qtail, htot);
                     pos = __shfl_sync(kFull, pos, 0) + hex;
@@ -167,6 +220,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
                     }
                 }
             }
+            quads += total;
             __syncthreads();
             head += m;
             tail = min(s.qtail, n);
@@ -175,9 +229,19 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         const uint32_t peeled = peeled0 + tail;
         if (tid == 0) {
             if (a.trace && it - 1 < a.trace_cap) {
+                // Tail rows: 0 level start (the first: this kernel's entry),
+                // 3 level end, 4 vertices peeled so far, 6 walk rounds, 7
+                // quads walked; 1, 2 and 5 = level end, except in the first
+                // row, which keeps the hand-off's times there (both barriers
+                // passed, CTA 0's fill done).
                 unsigned long long* row = a.trace + (size_t)(it - 1) * kTraceFields;
                 const unsigned long long t_end = now_ns();
-                row[0] = t_start; row[1] = t_end; row[2] = t_end; row[3] = t_end; row[4] = peeled; row[5] = t_end;
+                row[0] = it - 1 == it0 ? t_entry : t_start;
+                row[3] = t_end;
+                row[4] = peeled;
+                row[6] = rounds;
+                row[7] = quads;
+                if (it - 1 != it0) { row[1] = t_end; row[2] = t_end; row[5] = t_end; }
             }
             if (a.shells && level + 1 < a.shell_cap) a.shells[level + 1] = peeled;
         }

@@ -151,15 +151,16 @@ class DeviceGraph:
         return order[: self.V], shells[:nsh], k
 
     def trace(self):
-        """Per-level device trace -> (levels x 6) uint64 array: level start,
+        """Per-level device trace -> (levels x 8) uint64 array: level start,
         CTA 0 arrival, level complete, CTA 0 saw completion (ns), vertices
-        peeled so far, last CTA arrival (ns)."""
+        peeled so far, last CTA arrival (ns), walk rounds and adjacency quads
+        walked (levels of the one-CTA tail kernel; 0 for grid levels)."""
         maxdeg = int(np.diff(self.offsets).max()) if self.V else 0
-        buf = np.zeros((maxdeg + 2) * 6, np.uint64)
+        buf = np.zeros((maxdeg + 2) * 8, np.uint64)
         lv = C.c_uint32()
         check(lib().kc_graph_trace(self._h, buf.ctypes.data_as(C.POINTER(C.c_uint64)), maxdeg + 2,
                                    C.byref(lv)), "kc_graph_trace")
-        return buf.reshape(-1, 6)[: lv.value]
+        return buf.reshape(-1, 8)[: lv.value]
 
     def free(self) -> None:
         if getattr(self, "_h", None):
