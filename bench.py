@@ -34,9 +34,11 @@ sys.path.insert(0, str(ROOT))
 METRIC = "k-core edges/s & HBM GB/s; batched graphs/s, p50/p99 latency vs plain peel"
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
 
-# DRAM bytes per launch of the persistent peel kernel from one ncu capture of
-# the same workload (profiles/peel_persistent_*.md); None until captured.
-NCU_TRAFFIC = {}
+# DRAM bytes (read + write) of one peel -- the persistent kernel plus the
+# one-CTA tail kernel it hands the last levels to -- from one ncu capture of
+# the same workload (profiles/peel_persistent_rmat-s20-ef5.md); None where not
+# captured.
+NCU_TRAFFIC = {2: 45_161_472 + 4_132_096 + 7_796_480 + 0}
 
 
 def dist_env():
@@ -119,6 +121,8 @@ def reference_arm(args, rank, world):
     """The reference algorithm on the host cores (CPU restatement, all threads)."""
     if rank != 0:
         return
+    if args.config in (4, 5):
+        return reference_arm_graphs(args, world)
     from kcoregpu_gb300 import workloads as W
     from oracle import kc_oracle as O
     off, nbr = W.single_graph(args.config)
@@ -144,6 +148,53 @@ def reference_arm(args, rank, world):
                                    f"src/ours.cc:117-160, OpenMP, {cpu_model()})"},
         "e2e": {"value": val, "unit": "edges/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def reference_arm_graphs(args, world, sample: int = 48):
+    """Batched / served workloads on the host cores: the level-synchronous
+    restatement (all threads) over a bounded sample of the workload's graphs
+    (the first `sample` graphs of the batch, or requests of the stream),
+    reported as graphs/s."""
+    from kcoregpu_gb300 import workloads as W
+    from oracle import kc_oracle as O
+    nth = os.cpu_count() or 1
+    if args.config == 4:
+        seg = W.batch(sample)
+        graphs = [seg.graph(g) for g in range(seg.ngraphs)]
+        name, what = W.BATCH["name"], f"graphs 0..{sample - 1} of the batch"
+    else:
+        graphs = [W.served_request(i) for i in range(sample)]
+        name, what = W.SERVED["name"], f"requests 0..{sample - 1} of the stream (no scale-24 graph)"
+    for off, nbr in graphs[: max(1, args.warmup)]:
+        O.levelsync(off, nbr, nthreads=nth)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        for off, nbr in graphs:
+            O.levelsync(off, nbr, nthreads=nth)
+        times.append(time.perf_counter() - t0)
+    t = sum(times) / len(times)
+    val = len(graphs) / t
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "graphs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": name, "sample_graphs": len(graphs)},
+        "cpu_baseline": {"value": val, "unit": "graphs/s", "cores": nth, "kind": "port",
+                         "sample": f"{what}, level-synchronous restatement of src/ours.cc:117-160, "
+                                   f"OpenMP, {cpu_model()}"},
+        "e2e": {"value": val, "unit": "graphs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def max_over_ranks(values, world: int, device="cpu"):
+    """Element-wise maximum of per-rank timings (all_reduce MAX) -> list."""
+    if world <= 1:
+        return list(values)
+    import torch
+    t = torch.tensor(list(values), dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
 
 
 def cpu_baseline(off, nbr):
@@ -403,10 +454,7 @@ def main():
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = sum(step_ms) / len(step_ms)
     kms = sum(kern_ms) / len(kern_ms)
-    if world > 1:
-        t = torch.tensor([ms, kms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms, kms = t.tolist()
+    ms, kms = max_over_ranks([ms, kms], world, device="cuda")
 
     if args.profile:
         if rank == 0:
@@ -469,7 +517,7 @@ def main():
                      "traffic": NCU_TRAFFIC.get(args.config)},
         "e2e": {"value": world * m / e2e_s, "unit": "edges/s", "ms": e2e_s * 1e3,
                 "h2d_bytes_per_step": 4 * (V + 1) + 4 * arcs, "d2h_bytes_per_step": 4 * V},
-        "gpu_launches": args.steps,
+        "gpu_launches": 2 * args.steps,   # persistent peel + tail kernel per step
         "clocks": clk.summary(),
         "wall_s": t_wall,
     }
