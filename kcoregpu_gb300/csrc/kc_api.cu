@@ -151,6 +151,21 @@ void tail_limits(uint32_t* cap_v, uint32_t* cap_arcs) {
     *cap_arcs = arcs;
 }
 
+// Arcs a warp's cascade list may hold before the rest of a cascade is queued
+// for other warps (KC_LOCAL_BUDGET, default kLocalBudget).
+uint32_t local_budget() {
+    static uint32_t b = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        b = kLocalBudget;
+        if (const char* e = std::getenv("KC_LOCAL_BUDGET")) {
+            const long long x = std::atoll(e);
+            if (x >= 32 && x <= (1 << 20)) b = (uint32_t)x;
+        }
+    });
+    return b;
+}
+
 // Buffers of the tail hand-off for a graph of at most E arcs.
 int reserve_tail(kc_graph* g, uint64_t E) {
     uint32_t cap_v = 0, cap_arcs = 0;
@@ -335,6 +350,7 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     a.alive[1] = g->d_alive[1];
     a.trace = with_trace ? g->d_trace : nullptr;
     a.trace_cap = with_trace ? g->trace_cap : 0;
+    a.local_budget = local_budget();
     const bool tail = g->tail_cap_v != 0;
     if (tail) {
         a.tail_cap_v = g->tail_cap_v;

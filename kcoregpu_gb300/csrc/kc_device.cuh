@@ -41,6 +41,7 @@ constexpr uint32_t kClaim = 1u << 31;
 constexpr uint32_t kItemCap = 128;    // per-warp batch of arc ranges
 constexpr uint32_t kLocalArcs = 256;  // vertices with more arcs go to the task queue
 constexpr uint32_t kChunk = 256;      // arcs per queued task (len-1 fits 8 bits)
+constexpr uint32_t kLocalBudget = 128;   // arcs a warp's cascade list may hold; the rest is queued
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 
 // Device status codes (mirrors of KC_ERR_*; 0 = ok).
@@ -125,6 +126,7 @@ struct PeelArgs {
                                                // each adjacency padded to 4 entries with 0xFFFFFFFF)
     unsigned long long* tail_items = nullptr;  // fill work items: local id << 32 | arc chunk
     uint32_t tail_items_cap = 0;
+    uint32_t local_budget = kLocalBudget;      // arcs a warp's cascade list may hold
 };
 
 // Tail peel: one CTA of kTailThreads threads, states in shared memory.

@@ -67,6 +67,7 @@ struct Warp {
     uint32_t it;       // level iteration (levels may be skipped, iterations are consecutive)
     uint32_t minv;     // smallest survivor state this lane's scan saw
     uint32_t arcs;     // sum of the survivor degrees this lane's scan saw (tail hand-off only)
+    uint32_t narcs;    // arcs of the entries in the cascade list
 };
 
 // Optional per-level trace (kc_graph_trace): kTraceFields words per level.
@@ -110,21 +111,18 @@ __device__ __noinline__ void push_tasks(Warp& w, bool pred, uint32_t start, uint
     }
 }
 
-// Handles the vertices claimed by this warp in one walk step: records the
+// Handles the vertices claimed by this warp in one walk step (their arc
+// range [start, start+len) was loaded with the claiming atomic): records the
 // core number (and peel order), then queues their adjacency on the cascade
 // list or, for hubs and list overflow, on the global task queue.
-__device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u) {
+__device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u, uint32_t start, uint32_t len) {
     const unsigned m = __ballot_sync(kFull, found);
     if (!m) return;
     const unsigned lane = lane_id();
     const uint32_t cnt = __popc(m);
     w.peeled += cnt;
-    uint32_t start = 0, len = 0;
-    if (found && IN(u, w.a.V, 2)) {
-        w.a.core[u] = w.level;
-        start = KC_LDG(w.a.off + u);
-        len = KC_LDG(w.a.off + u + 1) - start;
-    }
+    if (!(found && IN(u, w.a.V, 2))) { start = 0; len = 0; }
+    else w.a.core[u] = w.level;
     if (w.a.order) {
         uint32_t pos = 0;
         if (lane == 0) pos = atomicAdd(&w.a.ctl->order_tail, cnt);
@@ -132,7 +130,13 @@ __device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u) {
         const uint32_t op = pos + __popc(m & lanemask_lt());
         if (found && IN(op, w.a.V, 4)) w.a.order[op] = u;
     }
+    // The cascade list keeps at most local_budget arcs: the rest of a wide
+    // cascade goes to the level's task queue, where idle warps take it,
+    // instead of being walked by this warp alone, 128 arcs a step.
     bool local = found && len <= kLocalArcs;
+    uint32_t lsum;
+    const uint32_t lex = warp_excl_scan(local ? len : 0u, &lsum);
+    if (local && w.narcs + lex + len > w.a.local_budget) local = false;
     unsigned lm = __ballot_sync(kFull, local);
     if (w.nnext + __popc(lm) > kItemCap) { local = false; lm = 0; }
     if (local) {
@@ -142,16 +146,36 @@ __device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u) {
         w.b.nlen[idx] = len;
     }
     w.nnext += __popc(lm);
+    w.narcs += __reduce_add_sync(kFull, local ? len : 0u);
     const bool glob = found && !local;
     if (__ballot_sync(kFull, glob)) push_tasks(w, glob, start, len);
 }
 
-// One neighbour u of a vertex peeled at this level (ours.cc:91-106): returns
-// true when this thread's decrement took u to the level and claimed it.
-__device__ __forceinline__ bool decrement(uint32_t* wp, uint32_t d, uint32_t kk) {
+// One neighbour u of a vertex peeled at this level (ours.cc:91-106), d its
+// state as read before: returns true when this thread's decrement took u to
+// the level and claimed it, with u's arc range in *start / *len.  When d says
+// the decrement will take u to the level, one atomicCAS decrements and claims
+// at once, and u's offsets are loaded while it is in flight: a cascade hop
+// waits for one atomic instead of a decrement, a claim and an offset load in
+// sequence.  A CAS that lost a race falls back to the reference's rule with
+// the value it saw.
+__device__ __forceinline__ bool decrement(const PeelArgs& a, uint32_t u, uint32_t d, uint32_t kk,
+                                          uint32_t* start, uint32_t* len) {
+    uint32_t* wp = a.w + u;
+    if (d == kk + 1) {
+        const uint32_t s0 = KC_LDG(a.off + u), s1 = KC_LDG(a.off + u + 1);
+        const uint32_t old = atomicCAS(wp, kk + 1, kClaim | kk);
+        if (old == kk + 1) { *start = s0; *len = s1 - s0; return true; }
+        d = old;
+    }
     if (!(d > kk && d < kClaim)) return false;
     const uint32_t old = atomicSub(wp, 1u);
-    if (old == kk + 1) return !(atomicOr(wp, kClaim) & kClaim);
+    if (old == kk + 1) {
+        const uint32_t s0 = KC_LDG(a.off + u), s1 = KC_LDG(a.off + u + 1);
+        if (atomicOr(wp, kClaim) & kClaim) return false;
+        *start = s0; *len = s1 - s0;
+        return true;
+    }
     if (old <= kk || old >= kClaim) atomicAdd(wp, 1u);   // undo (ours.cc:102-105)
     return false;
 }
@@ -209,9 +233,14 @@ __device__ void walk_items(Warp& w) {
         for (int j = 0; j < 4; ++j) d[j] = (u[j] != 0xFFFFFFFFu) ? __ldcg(w.a.w + u[j]) : 0u;
         bool f[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) f[j] = (u[j] != 0xFFFFFFFFu) && decrement(w.a.w + u[j], d[j], kk);
+        uint32_t cs[4], cl[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) on_claimed(w, f[j], u[j]);
+        for (int j = 0; j < 4; ++j) {
+            cs[j] = 0; cl[j] = 0;
+            f[j] = (u[j] != 0xFFFFFFFFu) && decrement(w.a, u[j], d[j], kk, &cs[j], &cl[j]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) on_claimed(w, f[j], u[j], cs[j], cl[j]);
     }
     __syncwarp();
 }
@@ -229,6 +258,7 @@ __device__ void walk_with_cascades(Warp& w) {
         }
         __syncwarp();
         w.nnext = 0;
+        w.narcs = 0;
         w.nitems = n;
         walk_items(w);
     }
@@ -818,7 +848,7 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
     __syncthreads();
 
     Warp w{a, sh.wb[wid], sh, nullptr, 0ull, 0u, kBias, 0u, 0u, 0u, nparts * kPeelWarps, nparts, kDense, 0u, 0u,
-           0u, kFull, 0u};
+           0u, kFull, 0u, 0u};
     const uint32_t gw = part * kPeelWarps + wid;
     PeelCtl* ctl = a.ctl;
     const bool lists = a.alive[0] != nullptr && a.alive[1] != nullptr;
