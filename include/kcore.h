@@ -242,6 +242,9 @@ typedef struct kc_serve_timing {
     double   latency_us;         /* submit -> core numbers on the host                   */
     uint32_t gang;               /* CTAs that peeled it                                  */
     uint32_t iterations;         /* level iterations run                                 */
+    double   copy_in_us;         /* device clock: job start -> CSR in device memory      */
+    double   peel_us;            /* device clock: CSR in -> peel done                    */
+    double   copy_out_us;        /* device clock: peel done -> result published          */
 } kc_serve_timing;
 
 typedef struct kc_serve_stats {
@@ -252,7 +255,8 @@ typedef struct kc_serve_stats {
     uint32_t pending;
     uint32_t inflight;
     uint32_t blocks;             /* CTAs of the serve kernel                             */
-    uint32_t pad;
+    uint32_t direct;             /* 1: jobs copy their CSR and result through the device's
+                                    access to pageable host memory, 0: pinned staging       */
 } kc_serve_stats;
 
 typedef struct kc_server kc_server;
@@ -260,7 +264,9 @@ typedef struct kc_server kc_server;
 int  kc_serve_open(const kc_serve_cfg* cfg, kc_server** s);   /* cfg may be NULL    */
 /* Queues a CSR (host arrays that must stay valid until the request completes);
  * the core numbers are written to core_out (V entries).  KC_ERR_BUDGET when the
- * request alone exceeds the budget, KC_ERR_CLOSED after kc_serve_close.        */
+ * request alone exceeds the budget, KC_ERR_CLOSED after kc_serve_close,
+ * KC_ERR_INVALID for offsets that do not start at 0 or decrease.  A neighbour
+ * id >= V fails the request with KC_ERR_INVALID (checked while it is copied). */
 int  kc_serve_submit(kc_server* s, const uint32_t* offsets, const uint32_t* neighbors,
                      uint32_t V, uint32_t* core_out, uint64_t* request_id);
 /* KC_OK (and forgets the request) once core_out holds the result, KC_ERR_BUSY

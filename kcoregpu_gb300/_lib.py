@@ -62,7 +62,8 @@ class ServeCfg(C.Structure):
 
 class ServeTiming(C.Structure):
     _fields_ = [("queue_us", C.c_double), ("latency_us", C.c_double), ("gang", C.c_uint32),
-                ("iterations", C.c_uint32)]
+                ("iterations", C.c_uint32), ("copy_in_us", C.c_double), ("peel_us", C.c_double),
+                ("copy_out_us", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -71,10 +72,10 @@ class ServeTiming(C.Structure):
 class ServeStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("in_use", C.c_uint64),
                 ("peak_in_use", C.c_uint64), ("pending", C.c_uint32), ("inflight", C.c_uint32),
-                ("blocks", C.c_uint32), ("pad", C.c_uint32)]
+                ("blocks", C.c_uint32), ("direct", C.c_uint32)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class BatchStats(C.Structure):

@@ -48,6 +48,7 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr int kErrOverflow = -4;
 constexpr int kErrTimeout = -5;
 constexpr int kErrCheck = -12;   // checked build: an index was out of bounds (access skipped)
+constexpr int kErrInvalid = -8;  // malformed input found on the device (a neighbour id >= V)
 
 // Counters of one level iteration.  A ring of 4 slots is reused: CTA 0 clears
 // the slot of iteration i-2 when it starts iteration i, when no warp can still

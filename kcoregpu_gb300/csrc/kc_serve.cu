@@ -19,6 +19,8 @@
 #include "kc_batch_impl.cuh"
 
 #include <algorithm>
+#include <cstdlib>
+#include <unistd.h>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -54,7 +56,11 @@ struct ServeJob {
     unsigned long long task_cap;
     PeelCtl* ctl;
     uint32_t* finished;          // gang members done
-    uint32_t pad[2];
+    uint32_t direct;             // 1: the gang copies the CSR in from, and the result out to, host memory
+    uint32_t pad;
+    const uint32_t* h_off;       // the request's host arrays (reached through the system page tables)
+    const uint32_t* h_nbr;
+    uint32_t* h_core;
 };
 
 static_assert(sizeof(ServeJob) % 8 == 0, "descriptors are copied in 8-byte words");
@@ -76,6 +82,10 @@ struct ServeDone {
     int err;
     uint32_t iters;
     uint32_t pad;
+    unsigned long long t_start;    // device clock (ns): the job's first CTA started
+    unsigned long long t_copied;   // the CSR was in device memory (all members)
+    unsigned long long t_peeled;   // the peel was done (all members)
+    unsigned long long t_out;      // the result was in host memory
 };
 
 struct ServeArgs {
@@ -99,6 +109,8 @@ struct ServeShared {
     unsigned long long ticket;
     int state;              // 1 = job found, 2 = stop, 3 = idle limit
     uint32_t kmax, iters;
+    int err;                // this CTA's job error (one-CTA jobs)
+    int bad;                // a neighbour id >= V was copied in
 };
 
 constexpr unsigned long long kNoSeq = ~0ull;
@@ -131,6 +143,39 @@ __device__ bool read_job(const ServeArgs& s, unsigned long long pos, ServeJob* o
     fence_acq_rel();
     const unsigned long long s2 = ld_sys64(&j->seq);
     return s2 == pos && out->seq == pos;
+}
+
+// Copies n 32-bit words from src to dst by the threads first, first+stride, ...
+// (16-byte words when both pointers allow).  Used for the request's host
+// arrays, which the device reads and writes through the system's page tables
+// (pageable memory access) at the host link's rate.  With limit != 0 it also
+// returns whether any word copied is >= limit (a neighbour id outside the
+// graph: the job is refused instead of peeled).
+__device__ bool copy_words(uint32_t* dst, const uint32_t* src, uint64_t n, uint64_t first, uint64_t stride,
+                           uint32_t limit = 0) {
+    bool bad = false;
+    if (((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+        const uint64_t n4 = n / 4;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        for (uint64_t i = first; i < n4; i += stride) {
+            const uint4 x = s4[i];
+            if (limit) bad |= (x.x >= limit) | (x.y >= limit) | (x.z >= limit) | (x.w >= limit);
+            d4[i] = x;
+        }
+        for (uint64_t i = n4 * 4 + first; i < n; i += stride) {
+            const uint32_t x = src[i];
+            if (limit) bad |= x >= limit;
+            dst[i] = x;
+        }
+    } else {
+        for (uint64_t i = first; i < n; i += stride) {
+            const uint32_t x = src[i];
+            if (limit) bad |= x >= limit;
+            dst[i] = x;
+        }
+    }
+    return bad;
 }
 
 __device__ void publish_done(const ServeArgs& s, const ServeJob& j, uint32_t kmax, int err, uint32_t iters) {
@@ -177,11 +222,30 @@ __global__ void __launch_bounds__(kPeelThreads, 2) serve_kernel(const __grid_con
         if (sh.state != 1) return;
         const ServeJob& j = sh.job;
         const unsigned long long t = sh.ticket;
+        ServeDone* dn = s.done + j.slot;
         if (j.gang <= 1) {
-            peel_graph_cta(j.off, j.nbr, j.core, j.V, s.queues + (size_t)blockIdx.x * s.qcap, s.qcap,
-                           &s.ctl->err, &sh.kmax, &sh.iters, sh.u.batch);
+            if (threadIdx.x == 0) { sh.err = 0; sh.kmax = 0; sh.iters = 0; dn->t_start = now_ns(); }
+            bool bad = false;
+            if (j.direct) {
+                copy_words(const_cast<uint32_t*>(j.off), j.h_off, (uint64_t)j.V + 1, threadIdx.x, blockDim.x);
+                bad = copy_words(const_cast<uint32_t*>(j.nbr), j.h_nbr, j.E, threadIdx.x, blockDim.x, j.V);
+            }
+            bad = __syncthreads_or(bad);
+            if (threadIdx.x == 0) dn->t_copied = now_ns();
+            if (bad) {
+                if (threadIdx.x == 0) sh.err = kErrInvalid;
+            } else {
+                peel_graph_cta(j.off, j.nbr, j.core, j.V, s.queues + (size_t)blockIdx.x * s.qcap, s.qcap,
+                               &sh.err, &sh.kmax, &sh.iters, sh.u.batch);
+            }
             __syncthreads();
-            if (threadIdx.x == 0) publish_done(s, j, sh.kmax, ld_err(&s.ctl->err), sh.iters);
+            if (threadIdx.x == 0) dn->t_peeled = now_ns();
+            if (j.direct && !sh.err) copy_words(j.h_core, j.core, j.V, threadIdx.x, blockDim.x);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                dn->t_out = now_ns();
+                publish_done(s, j, sh.kmax, sh.err, sh.iters);
+            }
         } else {
             PeelArgs a;
             a.off = j.off;
@@ -204,13 +268,30 @@ __global__ void __launch_bounds__(kPeelThreads, 2) serve_kernel(const __grid_con
             a.alive[1] = j.alive1;
             a.E = j.E;
             a.zero_tasks = 1;
-            peel_body(a, sh.u.peel, (uint32_t)(t - j.ticket0), j.gang);
+            const uint32_t part = (uint32_t)(t - j.ticket0);
+            const uint64_t first = (uint64_t)part * blockDim.x + threadIdx.x;
+            const uint64_t stride = (uint64_t)j.gang * blockDim.x;
+            bool ok = true;
+            if (part == 0 && threadIdx.x == 0) dn->t_start = now_ns();
+            if (j.direct) {   // the gang copies the CSR in, then starts together
+                copy_words(const_cast<uint32_t*>(j.off), j.h_off, (uint64_t)j.V + 1, first, stride);
+                const bool bad = copy_words(const_cast<uint32_t*>(j.nbr), j.h_nbr, j.E, first, stride, j.V);
+                if (__syncthreads_or(bad) && threadIdx.x == 0) record_error(j.ctl, kErrInvalid, 0);
+                ok = part_barrier(a, sh.u.peel, j.gang, 0);
+            }
+            if (part == 0 && threadIdx.x == 0) dn->t_copied = now_ns();
+            if (ok) peel_body(a, sh.u.peel, part, j.gang);
+            // every member is done: the gang copies the result out
+            const bool all_done = part_barrier(a, sh.u.peel, j.gang, 0);
+            if (part == 0 && threadIdx.x == 0) dn->t_peeled = now_ns();
+            if (j.direct && all_done && !ld_err(&j.ctl->err)) copy_words(j.h_core, j.core, j.V, first, stride);
             __syncthreads();
             if (threadIdx.x == 0) {
-                __threadfence();
+                __threadfence_system();   // this member's result words before its count
                 const unsigned fin = atomicAdd(j.finished, 1u) + 1u;
                 if (fin == j.gang) {
                     __threadfence();
+                    dn->t_out = now_ns();
                     publish_done(s, j, ld_relaxed(&j.ctl->kmax), ld_err(&j.ctl->err), ld_relaxed(&j.ctl->iterations));
                 }
             }
@@ -255,6 +336,7 @@ struct Request {
     int state = 0;           // 0 pending, 1 uploading, 2 running, 3 copying back, 4 done
     int err = 0;
     uint32_t kmax = 0, iters = 0;
+    double copy_in_us = 0, peel_us = 0, copy_out_us = 0;   // device clock
     clk::time_point t_submit, t_admit, t_publish, t_done;
 };
 
@@ -286,6 +368,12 @@ struct kc_server {
     unsigned char* dbg = nullptr;   // pinned scratch of kc_serve_debug
     uint32_t* h_zero = nullptr;     // pinned zero words (copy source of counter resets)
     bool kernel_running = false;
+    // The device reaches pageable host memory through the system page tables
+    // (cudaDevAttrPageableMemoryAccess): each job's gang then copies the CSR in
+    // and the result out itself, at the host link's rate and in parallel across
+    // jobs, and the staging above is not used (KC_SERVE_STAGED=1 forces it).
+    bool direct = false;
+    bool big_inflight = false;   // a gang of more than half the CTAs is running alone
     unsigned long long next_ticket = 0;
     unsigned long long next_seq = 0;
     uint64_t in_use = 0;
@@ -398,6 +486,7 @@ int device_alloc(kc_server* s, Request* r) {
         KC_CUDA(cudaMemcpyAsync(r->d_ctl, s->h_ctl_init, sizeof(PeelCtl), cudaMemcpyHostToDevice, s->cs));
         KC_CUDA(cudaMemcpyAsync(r->d_fin, s->h_zero, 4, cudaMemcpyHostToDevice, s->cs));
     }
+    if (s->direct) return KC_OK;   // the gang copies the CSR in
     int rc = stage_h2d(s, r->d_off, r->off, 4 * ((size_t)r->V + 1));
     if (rc == KC_OK && r->E) rc = stage_h2d(s, r->d_nbr, r->nbr, 4 * r->E);
     return rc;
@@ -461,13 +550,21 @@ bool loop_once(kc_server* s) {
     std::vector<Request*> admit;
     {
         std::lock_guard<std::mutex> lk(s->mu);
-        // admission, first come first served: stop at the first request that does
-        // not fit the budget or the ring
+        // Admission, first come first served: stop at the first request that
+        // does not fit the budget or the ring.  A big gang (more than half the
+        // CTAs) runs alone: it is admitted once nothing else is in flight, and
+        // nothing is admitted beside it -- its level chain waits for every
+        // member at every level, and members that share an SM with other jobs
+        // slowed it several-fold when it co-ran.
         while (!s->pending.empty()) {
             Request* r = s->pending.front();
+            if (s->big_inflight) break;
+            const bool big = 2 * r->gang > (uint32_t)s->grid;
+            if (big && !(s->inflight.empty() && admit.empty())) break;
             if (s->in_use + r->bytes > s->cfg.hbm_budget_bytes) break;
             if (s->inflight.size() + admit.size() >= s->cfg.ring_slots) break;
             s->pending.pop_front();
+            if (big) s->big_inflight = true;
             s->in_use += r->bytes;
             admit.push_back(r);
         }
@@ -476,7 +573,18 @@ bool loop_once(kc_server* s) {
     for (Request* r : admit) {
         r->t_admit = clk::now();
         int rc = device_alloc(s, r);
-        if (rc) { r->err = rc; r->state = 4; continue; }
+        if (rc) {   // the request fails alone; its budget share and a big gang's exclusivity are released
+            device_free(s, r);
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->in_use -= r->bytes;
+            if (2 * r->gang > (uint32_t)s->grid) s->big_inflight = false;
+            r->err = rc;
+            r->t_done = clk::now();
+            r->state = 4;
+            s->stats.completed++;
+            s->cv.notify_all();
+            continue;
+        }
         r->seq = s->next_seq++;
         const uint32_t slot = (uint32_t)(r->seq % s->cfg.ring_slots);
         ServeJob& j = s->h_ring[slot];
@@ -499,6 +607,10 @@ bool loop_once(kc_server* s) {
         j.task_cap = r->task_cap;
         j.ctl = r->d_ctl;
         j.finished = r->d_fin;
+        j.direct = s->direct ? 1u : 0u;
+        j.h_off = r->off;
+        j.h_nbr = r->nbr;
+        j.h_core = r->core_out;
         s->next_ticket += r->gang;
         s->h_tails[slot] = (unsigned)(r->seq + 1);
         publish(s, slot);
@@ -524,13 +636,16 @@ bool loop_once(kc_server* s) {
                 r->kmax = d.kmax;
                 r->err = d.err;
                 r->iters = d.iters;
+                r->copy_in_us = (d.t_copied - d.t_start) * 1e-3;
+                r->peel_us = (d.t_peeled - d.t_copied) * 1e-3;
+                r->copy_out_us = (d.t_out - d.t_peeled) * 1e-3;
                 r->state = 3;
                 finished.push_back(r);
             }
         }
     }
     for (Request* r : finished) {
-        if (r->V) {
+        if (r->V && !s->direct) {
             const int rc = stage_d2h(s, r->core_out, r->d_core, 4 * (size_t)r->V);
             if (rc && !r->err) r->err = rc;
         }
@@ -539,6 +654,7 @@ bool loop_once(kc_server* s) {
         std::lock_guard<std::mutex> lk(s->mu);
         s->in_use -= r->bytes;
         s->inflight.erase(std::find(s->inflight.begin(), s->inflight.end(), r));
+        if (2 * r->gang > (uint32_t)s->grid) s->big_inflight = false;
         r->state = 4;
         s->stats.completed++;
         progress = true;
@@ -620,6 +736,10 @@ int kc_serve_open(const kc_serve_cfg* cfg, kc_server** out) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)serve_kernel, kPeelThreads, 0);
     s->grid = sms * std::max(1, per);
     if (!s->cfg.max_gang || s->cfg.max_gang > (uint32_t)s->grid) s->cfg.max_gang = (uint32_t)s->grid;
+    int pageable = 0;
+    cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, s->dev);
+    const char* staged = std::getenv("KC_SERVE_STAGED");
+    s->direct = pageable == 1 && !(staged && std::atoi(staged) != 0);
     auto fail = [&](cudaError_t e, const char* w) { int rc = cuda_fail(e, w); delete s; return rc; };
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&s->ks, cudaStreamNonBlocking))) return fail(e, "stream");
@@ -669,10 +789,38 @@ int kc_serve_submit(kc_server* s, const uint32_t* offsets, const uint32_t* neigh
     r->V = V;
     r->E = V ? offsets[V] : 0;
     if (r->E && !neighbors) { delete r; return KC_ERR_INVALID; }
+    // Offsets must start at 0 and never decrease (the kernels trust arc
+    // ranges); with pinned staging the neighbour ids are checked here too,
+    // otherwise while the gang copies them in.
     uint32_t md = 0;
-    for (uint32_t v = 0; v < V; ++v) md = std::max(md, offsets[v + 1] - offsets[v]);
+    int bad = V && offsets[0] != 0;
+#pragma omp parallel for reduction(max : md) reduction(| : bad) schedule(static)
+    for (int64_t v = 0; v < (int64_t)V; ++v) {
+        if (offsets[v + 1] < offsets[v]) bad = 1;
+        else md = std::max(md, offsets[v + 1] - offsets[v]);
+    }
+    if (!bad && !s->direct) {
+#pragma omp parallel for reduction(| : bad) schedule(static)
+        for (int64_t e = 0; e < (int64_t)r->E; ++e) bad |= (neighbors[e] >= V);
+    }
+    if (bad || md >= (1u << 30)) {
+        delete r;
+        set_error_msg("invalid CSR: offsets must start at 0 and not decrease, neighbour ids must be < V, "
+                      "degrees below 2^30");
+        return KC_ERR_INVALID;
+    }
     r->maxdeg = md;
     r->core_out = core_out;
+    if (s->direct && V) {
+        // The device writes the result straight into core_out; a page the host
+        // never touched would be faulted in one device write at a time (about
+        // 5 GB/s measured), so every page is touched once here, in parallel.
+        const long ps = sysconf(_SC_PAGESIZE);
+        const size_t step = ps > 0 ? (size_t)ps / sizeof(uint32_t) : 1024;
+        const int64_t pages = (int64_t)(((size_t)V + step - 1) / step);
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < pages; ++i) core_out[(size_t)i * step] = 0;
+    }
     plan_request(s, r);
     if (r->bytes > s->cfg.hbm_budget_bytes) {
         delete r;
@@ -706,6 +854,9 @@ static void fill_timing(const Request* r, kc_serve_timing* t) {
     t->latency_us = us(r->t_submit, r->t_done);
     t->gang = r->gang;
     t->iterations = r->iters;
+    t->copy_in_us = r->copy_in_us;
+    t->peel_us = r->peel_us;
+    t->copy_out_us = r->copy_out_us;
 }
 
 int kc_serve_poll(kc_server* s, uint64_t id, uint32_t* kmax, kc_serve_timing* timing) {
@@ -782,6 +933,7 @@ int kc_serve_stats_get(kc_server* s, kc_serve_stats* st) {
     st->pending = (uint32_t)s->pending.size();
     st->inflight = (uint32_t)s->inflight.size();
     st->blocks = (uint32_t)s->grid;
+    st->direct = s->direct ? 1u : 0u;
     return KC_OK;
 }
 

@@ -51,20 +51,6 @@ __device__ __forceinline__ uint32_t tail_scan(uint32_t x, TailSmem& s, uint32_t*
     return s.warp_tot[wid] + ex;
 }
 
-// Appends the local ids v of the lanes with `pred` to the peel queue; every
-// lane of the warp calls it.
-__device__ __forceinline__ void tail_enqueue(TailSmem& s, bool pred, uint32_t v) {
-    const unsigned m = __ballot_sync(kFull, pred);
-    if (!m) return;
-    uint32_t pos = 0;
-    if ((threadIdx.x & 31) == 0) pos = atomicAdd(&s.qtail, (unsigned)__popc(m));
-    pos = __shfl_sync(kFull, pos, 0);
-    if (pred) {
-        const uint32_t p = pos + __popc(m & lanemask_lt());
-        if (p < kTailV) s.q[p] = v;
-    }
-}
-
 __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid_constant__ PeelArgs a) {
     extern __shared__ __align__(16) unsigned char tail_smem[];
     TailSmem& s = *reinterpret_cast<TailSmem*>(tail_smem);
@@ -120,9 +106,15 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
                 if (b + k < n && d[k] > level) mymin = min(mymin, d[k]);
                 if (b + k < n && d[k] == level) hit |= 1u << k;
             }
-            if (__any_sync(kFull, hit != 0)) {
+            if (__any_sync(kFull, hit != 0)) {   // one warp-aggregated append for the 4 states
+                uint32_t htot;
+                const uint32_t hex = warp_excl_scan(__popc(hit), &htot);
+                uint32_t pos = 0;
+                if (lane == 0) pos = atomicAdd(&s.qtail, htot);
+                pos = __shfl_sync(kFull, pos, 0) + hex;
 #pragma unroll
-                for (int k = 0; k < 4; ++k) tail_enqueue(s, (hit >> k) & 1u, b + k);
+                for (int k = 0; k < 4; ++k)
+                    if ((hit >> k) & 1u) { if (pos < kTailV) s.q[pos] = b + k; ++pos; }
             }
         }
         mymin = __reduce_min_sync(kFull, mymin);

@@ -72,3 +72,63 @@ def test_stream_of_small_requests(gpu):
         np.testing.assert_array_equal(core, wc)
         assert kmax == wk
     srv.close()
+
+
+@pytest.mark.parametrize("staged", ["0", "1"])
+def test_direct_and_staged_transfers_agree(gpu, monkeypatch, staged):
+    # On devices that reach pageable host memory the gangs copy each request's
+    # CSR in and its result out themselves; KC_SERVE_STAGED=1 forces the pinned
+    # staging path.  Both must give the oracle's results, for arrays with and
+    # without 16-byte alignment.
+    monkeypatch.setenv("KC_SERVE_STAGED", staged)
+    gs = mix()[:9]
+    o, n = gs[6]
+    buf = np.empty(len(n) + 1, np.uint32)     # neighbours at a 4-byte (not 16-byte) offset
+    buf[1:] = n
+    gs.append((o, buf[1:]))
+    srv = Server()
+    direct = srv.stats()["direct"]
+    if staged == "1":
+        assert direct == 0
+    ids = [srv.submit(o, n) for o, n in gs]
+    res = [srv.wait(r) for r in ids]
+    srv.close()
+    for (o, n), (core, kmax, _) in zip(gs, res):
+        wc, wk = O.bz(o, n)
+        np.testing.assert_array_equal(core, wc)
+        assert kmax == wk
+
+
+@pytest.mark.parametrize("staged", ["0", "1"])
+def test_malformed_requests_are_refused_and_the_server_continues(gpu, monkeypatch, staged):
+    # A neighbour id >= V is refused before any kernel indexes with it: on the
+    # host with pinned staging, while the gang copies the CSR in otherwise (for
+    # a one-CTA job and for a gang).  Decreasing offsets fail the submit.
+    monkeypatch.setenv("KC_SERVE_STAGED", staged)
+    srv = Server()
+    small = kc.build_csr(*kc.gen_er(5000, 20000, 77))[:2]
+    big = kc.build_csr(*kc.gen_rmat(1 << 20, 6 << 20, 78))[:2]
+    for o, n in (small, big):
+        bad = n.copy()
+        bad[len(bad) // 2] = len(o) - 1 + 5     # >= V
+        if staged == "1":
+            with pytest.raises(KCoreError) as e:
+                srv.submit(o, bad)
+        else:
+            rid = srv.submit(o, bad)
+            with pytest.raises(KCoreError) as e:
+                srv.wait(rid)
+        assert e.value.name == "KC_ERR_INVALID"
+    o, n = small
+    dec = o.copy()
+    dec[11] = dec[10] - 1                    # offsets decrease
+    with pytest.raises(KCoreError) as e:
+        srv.submit(dec, n)
+    assert e.value.name == "KC_ERR_INVALID"
+    for o, n in (small, big):    # the server still serves
+        core, kmax, t = srv.wait(srv.submit(o, n))
+        wc, wk = O.bz(o, n)
+        np.testing.assert_array_equal(core, wc)
+        assert kmax == wk
+        assert t["peel_us"] > 0
+    srv.close()
