@@ -77,10 +77,19 @@ void kc_csr_free(kc_csr_host* csr);
 int  kc_read_serialized(const char* path, kc_csr_host* out);
 int  kc_write_serialized(const char* path, const kc_csr_host* csr);
 
+/* Binary CSR sidecar of the serialized cache (no reference counterpart: it
+ * cuts load time): "KCCSRBN1", V (uint32), 0 (uint32), E (uint64), then the raw
+ * offsets[V+1] and neighbors[E] (uint32, host byte order).  The reader
+ * validates sizes, offsets and neighbour ids (KC_ERR_PARSE otherwise).          */
+int  kc_write_csr_binary(const char* path, const kc_csr_host* csr);
+int  kc_read_csr_binary(const char* path, kc_csr_host* out);
+
 /* Graph::Graph(path) (graph.cpp:142-154): read <cache_dir>/serialized-<basename>
  * when present, else parse the text and write that cache (silently skipped when
  * cache_dir is missing).  cache_dir NULL means "./output/" (inc/common.h:17).
- * *from_cache is set to 1 when the cache was used (may be NULL).                */
+ * Beside the text cache a binary sidecar serialized-<basename>.kcb is written
+ * and, unless the text cache is newer, read instead of it.  *from_cache is set
+ * to 1 when the text cache was used, 2 for the sidecar (may be NULL).           */
 int  kc_load_graph(const char* path, const char* cache_dir, int parse_mode,
                    kc_csr_host* out, int* from_cache);
 

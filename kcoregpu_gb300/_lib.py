@@ -98,6 +98,8 @@ SIGNATURES = {
     "kc_csr_free": (None, [C.POINTER(CsrHost)]),
     "kc_read_serialized": (C.c_int, [_cp, C.POINTER(CsrHost)]),
     "kc_write_serialized": (C.c_int, [_cp, C.POINTER(CsrHost)]),
+    "kc_read_csr_binary": (C.c_int, [_cp, C.POINTER(CsrHost)]),
+    "kc_write_csr_binary": (C.c_int, [_cp, C.POINTER(CsrHost)]),
     "kc_load_graph": (C.c_int, [_cp, _cp, C.c_int, C.POINTER(CsrHost), C.POINTER(C.c_int)]),
     "kc_write_core_json": (C.c_int, [_cp, _u32p, C.c_uint32]),
     "kc_write_core_txt": (C.c_int, [_cp, _u32p, C.c_uint32]),

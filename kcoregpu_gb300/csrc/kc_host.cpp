@@ -382,25 +382,105 @@ int kc_read_serialized(const char* path, kc_csr_host* out) {
     return KC_OK;
 }
 
+// Binary CSR sidecar: a 24-byte header (8-byte magic, V, 0, E as uint64) and
+// the raw offsets[V+1] and neighbors[E] (uint32, host byte order).  Reading
+// it is a block read plus a validation pass; the text cache needs a parse.
+static const char kBinMagic[8] = {'K', 'C', 'C', 'S', 'R', 'B', 'N', '1'};
+
+int kc_write_csr_binary(const char* path, const kc_csr_host* csr) {
+    if (!path || !csr || (csr->V && !csr->offsets) || (csr->E && !csr->neighbors))
+        return fail(KC_ERR_INVALID, "null argument");
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(KC_ERR_IO, std::string("cannot write ") + path);
+    const uint32_t hv[2] = {csr->V, 0};
+    const uint64_t e = csr->E;
+    bool ok = std::fwrite(kBinMagic, 1, 8, f) == 8 && std::fwrite(hv, 4, 2, f) == 2 && std::fwrite(&e, 8, 1, f) == 1;
+    static const uint32_t zero = 0;
+    if (ok) ok = csr->V ? std::fwrite(csr->offsets, 4, (size_t)csr->V + 1, f) == (size_t)csr->V + 1
+                        : std::fwrite(&zero, 4, 1, f) == 1;
+    if (ok && e) ok = std::fwrite(csr->neighbors, 4, e, f) == e;
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) { std::remove(path); return fail(KC_ERR_IO, "write failed"); }
+    return KC_OK;
+}
+
+int kc_read_csr_binary(const char* path, kc_csr_host* out) {
+    if (!path || !out) return fail(KC_ERR_INVALID, "null argument");
+    std::memset(out, 0, sizeof(*out));
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(KC_ERR_IO, std::string("cannot open ") + path);
+    char magic[8];
+    uint32_t hv[2];
+    uint64_t E = 0;
+    if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kBinMagic, 8) != 0 || std::fread(hv, 4, 2, f) != 2 ||
+        std::fread(&E, 8, 1, f) != 1 || E > 0xFFFFFFFFull) {
+        std::fclose(f);
+        return fail(KC_ERR_PARSE, "binary CSR: bad header");
+    }
+    const uint32_t V = hv[0];
+    uint32_t* deg = (uint32_t*)std::malloc(sizeof(uint32_t) * (V ? V : 1));
+    uint32_t* off = (uint32_t*)std::malloc(sizeof(uint32_t) * ((size_t)V + 1));
+    uint32_t* nbr = (uint32_t*)std::malloc(sizeof(uint32_t) * (E ? E : 1));
+    bool ok = deg && off && nbr;
+    if (ok) ok = std::fread(off, 4, (size_t)V + 1, f) == (size_t)V + 1;
+    if (ok && E) ok = std::fread(nbr, 4, E, f) == E;
+    if (ok) ok = std::fgetc(f) == EOF;   // nothing after the arrays
+    std::fclose(f);
+    if (ok) ok = off[0] == 0 && off[V] == E;
+    int bad = !ok;
+    if (ok) {
+#pragma omp parallel for reduction(| : bad) schedule(static)
+        for (int64_t i = 0; i < (int64_t)V; ++i) {
+            if (off[i + 1] < off[i]) bad = 1;
+            else deg[i] = off[i + 1] - off[i];
+        }
+#pragma omp parallel for reduction(| : bad) schedule(static)
+        for (int64_t i = 0; i < (int64_t)E; ++i) bad |= nbr[i] >= V;
+    }
+    if (bad) {
+        std::free(deg); std::free(off); std::free(nbr);
+        return fail(KC_ERR_PARSE, "binary CSR: truncated or inconsistent");
+    }
+    out->V = V; out->E = (uint32_t)E; out->degrees = deg; out->offsets = off; out->neighbors = nbr;
+    return KC_OK;
+}
+
+static bool is_dir(const std::string& d) {
+    struct stat st;
+    return !d.empty() && stat(d.c_str(), &st) == 0 && S_ISDIR(st.st_mode);
+}
+
 int kc_load_graph(const char* path, const char* cache_dir, int mode, kc_csr_host* out, int* from_cache) {
     if (!path || !out) return fail(KC_ERR_INVALID, "null argument");
     if (from_cache) *from_cache = 0;
-    std::string cache = join_dir(cache_dir, std::string("serialized-") + basename_of(path));
-    FILE* f = std::fopen(cache.c_str(), "rb");
-    if (f) {
-        std::fclose(f);
+    const std::string cache = join_dir(cache_dir, std::string("serialized-") + basename_of(path));
+    const std::string side = cache + ".kcb";
+    const std::string dir = cache.substr(0, cache.find_last_of('/') + 1);
+    struct stat tst, bst;
+    const bool have_text = stat(cache.c_str(), &tst) == 0;
+    const bool have_bin = stat(side.c_str(), &bst) == 0;
+    // The sidecar stands for the text cache it was written with: it is used
+    // unless the text cache is newer (rewritten since).
+    if (have_bin && (!have_text || bst.st_mtime >= tst.st_mtime)) {
+        if (kc_read_csr_binary(side.c_str(), out) == KC_OK) {
+            if (from_cache) *from_cache = 2;
+            return KC_OK;
+        }
+    }
+    if (have_text) {
         int rc = kc_read_serialized(cache.c_str(), out);
-        if (rc == KC_OK && from_cache) *from_cache = 1;
+        if (rc == KC_OK) {
+            if (from_cache) *from_cache = 1;
+            if (is_dir(dir)) (void)kc_write_csr_binary(side.c_str(), out);
+        }
         return rc;
     }
     int rc = kc_load_edgelist(path, mode, out);
     if (rc) return rc;
     // writeSerialized() silently gives up when the output directory is missing
-    // (graph.cpp:38-53); so does this.
-    std::string dir = cache.substr(0, cache.find_last_of('/') + 1);
-    struct stat st;
-    if (!dir.empty() && stat(dir.c_str(), &st) == 0 && S_ISDIR(st.st_mode))
-        (void)kc_write_serialized(cache.c_str(), out);
+    // (graph.cpp:38-53); so does this (the text cache first, then its sidecar).
+    if (is_dir(dir) && kc_write_serialized(cache.c_str(), out) == KC_OK)
+        (void)kc_write_csr_binary(side.c_str(), out);
     return KC_OK;
 }
 

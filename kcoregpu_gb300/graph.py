@@ -54,6 +54,19 @@ def write_serialized(path: str, offsets, neighbors, degrees=None) -> None:
     check(lib().kc_write_serialized(os.fsencode(path), C.byref(c)), "kc_write_serialized")
 
 
+def read_csr_binary(path: str):
+    """Binary CSR sidecar -> (offsets, neighbors, degrees)."""
+    c = L.CsrHost()
+    check(lib().kc_read_csr_binary(os.fsencode(path), C.byref(c)), "kc_read_csr_binary")
+    return L.csr_to_numpy(c)
+
+
+def write_csr_binary(path: str, offsets, neighbors) -> None:
+    off, nbr = u32(offsets), u32(neighbors)
+    c = L.numpy_to_csr(off, nbr, u32(np.diff(off)))
+    check(lib().kc_write_csr_binary(os.fsencode(path), C.byref(c)), "kc_write_csr_binary")
+
+
 def write_core_json(path: str, core) -> None:
     """Graph::writeKCoreToDisk bytes (graph.cpp:126-140)."""
     c = u32(core)
@@ -198,6 +211,7 @@ class Graph:
         self.kmax = 0
         self.core = None
         self.from_cache = False
+        self.cache_kind = 0   # 1: text serialized cache, 2: its binary sidecar
         self.cache_dir = cache_dir
         self.parse_mode = parse_mode
         if input_file is not None:
@@ -210,6 +224,7 @@ class Graph:
                   "kc_load_graph")
             self._set(*L.csr_to_numpy(c))
             self.from_cache = bool(hit.value)
+            self.cache_kind = hit.value
 
     def _set(self, off, nbr, deg):
         self.neighbors_offset, self.neighbors, self.degrees = off, nbr, deg

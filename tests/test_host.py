@@ -82,9 +82,42 @@ def test_graph_cache_roundtrip(tmp_path):
     assert not g1.from_cache
     assert (outdir / "serialized-g.txt").read_bytes() == (GOLDEN / "serialized-skew_300.txt").read_bytes()
     g2 = kc.Graph(str(src), cache_dir=str(outdir))
-    assert g2.from_cache
+    assert g2.from_cache and g2.cache_kind == 2      # the binary sidecar written beside it
     np.testing.assert_array_equal(g1.neighbors, g2.neighbors)
+    np.testing.assert_array_equal(g1.neighbors_offset, g2.neighbors_offset)
+    np.testing.assert_array_equal(g1.degrees, g2.degrees)
     assert g2.V == g1.V and g2.E == g1.E
+    # a text cache rewritten after the sidecar wins over it (and refreshes it)
+    side = outdir / "serialized-g.txt.kcb"
+    os.utime(side, (1, 1))
+    g3 = kc.Graph(str(src), cache_dir=str(outdir))
+    assert g3.cache_kind == 1
+    np.testing.assert_array_equal(g1.neighbors, g3.neighbors)
+    assert kc.Graph(str(src), cache_dir=str(outdir)).cache_kind == 2
+
+
+@pytest.mark.parametrize("name", ["k5", "skew_300"])
+def test_binary_sidecar_roundtrip_and_rejects(name, tmp_path):
+    off, nbr, deg = golden_serialized(name)
+    p = tmp_path / "g.kcb"
+    kc.write_csr_binary(str(p), off, nbr)
+    o2, n2, d2 = kc.read_csr_binary(str(p))
+    np.testing.assert_array_equal(o2, off)
+    np.testing.assert_array_equal(n2, nbr)
+    np.testing.assert_array_equal(d2, deg)
+    raw = p.read_bytes()
+    bad = tmp_path / "bad.kcb"
+    for blob in (raw[:-4], raw + b"x", b"XXXXXXXX" + raw[8:]):   # truncated, trailing, magic
+        bad.write_bytes(blob)
+        with pytest.raises(KCoreError) as e:
+            kc.read_csr_binary(str(bad))
+        assert e.value.name == "KC_ERR_PARSE"
+    # a neighbour id >= V
+    arr = bytearray(raw)
+    arr[-4:] = (len(off) + 7).to_bytes(4, "little")
+    bad.write_bytes(bytes(arr))
+    with pytest.raises(KCoreError):
+        kc.read_csr_binary(str(bad))
 
 
 def test_graph_cache_dir_missing_is_silent(tmp_path):
