@@ -31,6 +31,7 @@ struct TailSmem {
     uint32_t qtail;
     uint32_t minv;
     uint32_t total;
+    uint32_t level_start;             // qtail when the level began (set before the level's barrier)
 };
 
 // Block-wide exclusive prefix sum of one value per thread.
@@ -89,9 +90,14 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
     bool failed = false;
     for (;;) {
         unsigned long long t_start = 0;
-        if (tid == 0) { s.minv = kFull; if (a.trace) t_start = now_ns(); }
+        if (tid == 0) {
+            s.minv = kFull;
+            s.level_start = s.qtail;
+            if (a.trace) t_start = now_ns();
+        }
         __syncthreads();
-        const uint32_t lvl_start = s.qtail;
+        // a snapshot taken before the barrier: the scan below appends at once
+        const uint32_t lvl_start = s.level_start;
         // scan: every vertex whose degree equals the level (ours.cc:15-25);
         // peeled vertices keep the level they were peeled at, below this one
         uint32_t mymin = kFull;
