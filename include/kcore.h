@@ -241,7 +241,7 @@ void kc_segcsr_free(kc_segcsr_host* s);
 typedef struct kc_serve_cfg {
     uint64_t hbm_budget_bytes;   /* device memory the admitted requests may hold (0: 64 GiB) */
     uint32_t ring_slots;         /* max requests admitted at once (0: 1024)              */
-    uint32_t gang_arcs;          /* arcs per gang CTA (0: 2^21)                           */
+    uint32_t gang_arcs;          /* arcs per gang CTA (0: 2^19)                           */
     uint32_t max_gang;           /* largest gang (0: every CTA of the kernel)             */
     uint32_t small_vertices;     /* largest graph one CTA may peel alone (0: 2^18)        */
 } kc_serve_cfg;

@@ -17,6 +17,7 @@ struct BatchShared {
     uint32_t start[kBatchChunk];     // first arc of each item
     uint32_t warp_tot[kBatchWarps];
     uint32_t qtail;                  // vertices peeled so far in this graph
+    uint32_t level_start;            // qtail when the level began (set before the level's barrier)
     uint32_t minv;                   // smallest survivor degree seen by a level's scan
     uint32_t g;                      // schedule index of the current graph
 };
@@ -51,16 +52,6 @@ __device__ __forceinline__ void enqueue(BatchShared& sh, uint32_t* q, bool pred,
     if (pred) q[pos + __popc(m & lanemask_lt())] = v;
 }
 
-// One neighbour u of a vertex peeled at `level` (ours.cc:91-106).  Returns
-// true when this decrement took u to the level (u joins this level).
-__device__ __forceinline__ bool step(uint32_t* w, uint32_t u, uint32_t level) {
-    if (__ldcg(w + u) <= level) return false;
-    const uint32_t old = atomicSub(w + u, 1u);
-    if (old == level + 1) return true;
-    if (old <= level) atomicAdd(w + u, 1u);   // undo (ours.cc:102-105)
-    return false;
-}
-
 // Peels one graph (V vertices, graph-local CSR off/nb) with this CTA alone.
 // w (V entries) receives the core numbers, q (>= V entries) is the CTA's
 // queue / peel order.  Thread 0 writes kmax and the level iterations run.
@@ -76,23 +67,45 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
         if (tid == 0) atomicCAS(err, 0, kErrOverflow);
         return;
     }
-    for (uint32_t v = tid; v < V; v += kBatchThreads) w[v] = KC_LDG(off + v + 1) - KC_LDG(off + v);
+    for (uint32_t b = 0; b < V; b += 4 * kBatchThreads) {
+        uint32_t o[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t v = b + k * kBatchThreads + tid;
+            o[k] = v < V ? KC_LDG(off + v + 1) - KC_LDG(off + v) : 0u;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t v = b + k * kBatchThreads + tid;
+            if (v < V) w[v] = o[k];
+        }
+    }
     if (tid == 0) sh.qtail = 0;
     __syncthreads();
 
     uint32_t level = 0, iters = 0;
     for (;;) {
-        if (tid == 0) sh.minv = kFull;
+        if (tid == 0) { sh.minv = kFull; sh.level_start = sh.qtail; }
         __syncthreads();
-        const uint32_t lvl_start = sh.qtail;
-        // scan: every vertex whose degree equals the level (ours.cc:15-25)
+        // a snapshot taken before the barrier: the scan below appends at once
+        const uint32_t lvl_start = sh.level_start;
+        // scan: every vertex whose degree equals the level (ours.cc:15-25),
+        // kScanLoads independent loads in flight per thread
+        constexpr uint32_t kScanLoads = 8;
         uint32_t mymin = kFull;
-        for (uint32_t base = 0; base < V; base += kBatchThreads) {
-            const uint32_t v = base + tid;
-            uint32_t d = kFull;
-            if (v < V) d = __ldcg(w + v);
-            if (d != kFull && d > level) mymin = min(mymin, d);
-            enqueue(sh, q, v < V && d == level, v);
+        for (uint32_t base = 0; base < V; base += kBatchThreads * kScanLoads) {
+            uint32_t d[kScanLoads];
+#pragma unroll
+            for (uint32_t k = 0; k < kScanLoads; ++k) {
+                const uint32_t v = base + k * kBatchThreads + tid;
+                d[k] = v < V ? __ldcg(w + v) : kFull;
+            }
+#pragma unroll
+            for (uint32_t k = 0; k < kScanLoads; ++k) {
+                const uint32_t v = base + k * kBatchThreads + tid;
+                if (d[k] != kFull && d[k] > level) mymin = min(mymin, d[k]);
+                enqueue(sh, q, v < V && d[k] == level, v);
+            }
         }
         mymin = __reduce_min_sync(kFull, mymin);
         if ((tid & 31) == 0 && mymin != kFull) atomicMin(&sh.minv, mymin);
@@ -115,12 +128,16 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
             __syncthreads();
             if (tid == 0) sh.pref[n] = total;
             __syncthreads();
+            // kWalkArcs arcs per thread: neighbour ids, then degree pre-checks,
+            // then the atomics, each group in flight together
+            constexpr int kWalkArcs = 4;
             uint32_t lo = 0;
-            for (uint32_t b = 0; b < total; b += 2 * kBatchThreads) {
-                uint32_t u[2] = {kFull, kFull};
+            for (uint32_t b = 0; b < total; b += kWalkArcs * kBatchThreads) {
+                uint32_t u[kWalkArcs];
 #pragma unroll
-                for (int j = 0; j < 2; ++j) {
+                for (int j = 0; j < kWalkArcs; ++j) {
                     const uint32_t arc = b + j * kBatchThreads + tid;
+                    u[j] = kFull;
                     if (arc < total) {
                         uint32_t hi = n;
                         while (hi - lo > 1) {
@@ -130,10 +147,19 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
                         u[j] = KC_LDG(nb + sh.start[lo] + (arc - sh.pref[lo]));
                     }
                 }
+                uint32_t d[kWalkArcs];
 #pragma unroll
-                for (int j = 0; j < 2; ++j) {
-                    const bool f = u[j] != kFull && step(w, u[j], level);
-                    enqueue(sh, q, f, u[j]);
+                for (int j = 0; j < kWalkArcs; ++j) d[j] = u[j] < V ? __ldcg(w + u[j]) : 0u;
+                uint32_t old[kWalkArcs];
+#pragma unroll
+                for (int j = 0; j < kWalkArcs; ++j) old[j] = (u[j] < V && d[j] > level) ? atomicSub(w + u[j], 1u) : 0u;
+#pragma unroll
+                for (int j = 0; j < kWalkArcs; ++j) {
+                    // (ours.cc:91-106): the decrement that took u to the level
+                    // queues it; one that raced below the level is undone
+                    const bool live = u[j] < V && d[j] > level;
+                    if (live && old[j] <= level) atomicAdd(w + u[j], 1u);
+                    enqueue(sh, q, live && old[j] == level + 1, u[j]);
                 }
             }
             __syncthreads();

@@ -371,29 +371,68 @@ __device__ void scan_level(Warp& w, uint32_t gw) {
     if (w.mode == kList || w.mode == kListCompact) {
         const uint32_t* list = a.alive[w.list_cur];
         const uint32_t n = w.list_len;
-        for (uint32_t i0 = gw * 32; i0 < n; i0 += w.nwt * 32) {
-            const uint32_t i = i0 + lane;
-            uint32_t v[4] = {0, 0, 0, 0};
-            uint32_t d = kClaim;
-            if (i < n && IN(i, a.V, 13)) {
-                v[0] = __ldcg(list + i);
-                if (v[0] < a.V) d = __ldcg(a.w + v[0]);
-                else record_error(a.ctl, kErrOverflow, w.level);   // defensive: never index past V
+        // When every warp has several steps of the list (a small gang), a step
+        // takes 128 entries, 4 per lane with their loads in flight together;
+        // otherwise 32, one per lane, so that a short list still spreads over
+        // all warps.
+        const uint32_t nj = (n >= w.nwt * 128u * 2u) ? 4u : 1u;
+        for (uint32_t i0 = gw * 32 * nj; i0 < n; i0 += w.nwt * 32 * nj) {
+            uint32_t v[4];
+#pragma unroll
+            for (uint32_t j = 0; j < 4; ++j) {
+                const uint32_t i = i0 + j * 32 + lane;
+                v[j] = (j < nj && i < n && IN(i, a.V, 13)) ? __ldcg(list + i) : kFull;
             }
-            const unsigned hit = (d == kk) ? 1u : 0u;
-            const bool sv = d > kk && d < kClaim;
-            if (sv) { w.minv = min(w.minv, d); w.arcs += d - kBias; }
-            if (compact) append_survivors(w, v, sv ? 1u : 0u);
+            uint32_t d[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                d[j] = kClaim;
+                if (v[j] < a.V) d[j] = __ldcg(a.w + v[j]);
+                else if (v[j] != kFull) record_error(a.ctl, kErrOverflow, w.level);   // defensive: never index past V
+            }
+            unsigned hit = 0, surv = 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                if (d[j] == kk) hit |= 1u << j;
+                if (d[j] > kk && d[j] < kClaim) { surv |= 1u << j; w.minv = min(w.minv, d[j]); w.arcs += d[j] - kBias; }
+            }
+            if (compact) append_survivors(w, v, surv);
             if (!__ballot_sync(kFull, hit != 0)) continue;
             after_claims(w, v, claim_hits(w, v, hit));
         }
     } else {
         const uint32_t ngroups = (a.V + 127) / 128;
         uint4* w4 = reinterpret_cast<uint4*>(a.w);
-        for (uint32_t g = gw; g < ngroups; g += w.nwt) {
+        // When every warp has several groups (a small gang), a step takes two
+        // 128-vertex groups with both loads in flight together.
+        const uint4 kNone = make_uint4(kClaim, kClaim, kClaim, kClaim);
+        const uint32_t ng = (ngroups >= 4 * w.nwt) ? 2u : 1u;
+        for (uint32_t g0 = gw; w.level != 0 && g0 < ngroups; g0 += ng * w.nwt) {
+            const uint32_t g1 = g0 + w.nwt;
+            uint4 xg[2];
+            xg[0] = IN(g0 * 32 + lane, (a.V + 127) / 128 * 32, 18) ? __ldcg(w4 + g0 * 32 + lane) : kNone;
+            xg[1] = (ng == 2 && g1 < ngroups && IN(g1 * 32 + lane, (a.V + 127) / 128 * 32, 18)) ? __ldcg(w4 + g1 * 32 + lane)
+                                                                                                : kNone;
+#pragma unroll
+            for (uint32_t r = 0; r < 2; ++r) {
+                if (r >= ng) break;
+                const uint32_t vb = (r ? g1 : g0) * 128 + lane * 4;
+                const uint32_t v[4] = {vb, vb + 1, vb + 2, vb + 3};
+                const uint32_t xs[4] = {xg[r].x, xg[r].y, xg[r].z, xg[r].w};
+                unsigned hit = 0, surv = 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (xs[j] == kk) hit |= 1u << j;
+                    if (xs[j] > kk && xs[j] < kClaim) { surv |= 1u << j; w.minv = min(w.minv, xs[j]); w.arcs += xs[j] - kBias; }
+                }
+                if (compact) append_survivors(w, v, surv);
+                if (__ballot_sync(kFull, hit != 0)) after_claims(w, v, claim_hits(w, v, hit));
+            }
+        }
+        for (uint32_t g = gw; w.level == 0 && g < ngroups; g += w.nwt) {
             const uint32_t vb = g * 128 + lane * 4;
             const uint32_t v[4] = {vb, vb + 1, vb + 2, vb + 3};
-            if (w.level == 0) {
+            {
                 // Level 0 also initialises the state from the offsets: isolated
                 // vertices are peeled here and have nothing to walk.
                 uint32_t st[4];
@@ -416,20 +455,7 @@ __device__ void scan_level(Warp& w, uint32_t gw) {
                     if (!(st[j] & kClaim)) { surv |= 1u << j; w.minv = min(w.minv, st[j]); w.arcs += st[j] - kBias; }
                 if (compact) append_survivors(w, v, surv);
                 after_claims(w, v, mine);
-                continue;
             }
-            const uint4 x = IN(g * 32 + lane, (a.V + 127) / 128 * 32, 18) ? __ldcg(w4 + g * 32 + lane)
-                                                                         : make_uint4(kClaim, kClaim, kClaim, kClaim);
-            const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
-            unsigned hit = 0, surv = 0;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                if (xs[j] == kk) hit |= 1u << j;
-                if (xs[j] > kk && xs[j] < kClaim) { surv |= 1u << j; w.minv = min(w.minv, xs[j]); w.arcs += xs[j] - kBias; }
-            }
-            if (compact) append_survivors(w, v, surv);
-            if (!__ballot_sync(kFull, hit != 0)) continue;
-            after_claims(w, v, claim_hits(w, v, hit));
         }
     }
     walk_with_cascades(w);

@@ -188,7 +188,7 @@ __device__ void publish_done(const ServeArgs& s, const ServeJob& j, uint32_t kma
     __threadfence_system();
 }
 
-__global__ void __launch_bounds__(kPeelThreads, 2) serve_kernel(const __grid_constant__ ServeArgs s) {
+__global__ void __launch_bounds__(kPeelThreads, 1) serve_kernel(const __grid_constant__ ServeArgs s) {
     __shared__ ServeShared sh;
     unsigned long long cursor = s.cursor0;   // ring position: jobs before it end below this CTA's tickets
     for (;;) {
@@ -728,7 +728,7 @@ int kc_serve_open(const kc_serve_cfg* cfg, kc_server** out) {
     if (cfg) s->cfg = *cfg;
     if (!s->cfg.hbm_budget_bytes) s->cfg.hbm_budget_bytes = 64ull << 30;
     if (!s->cfg.ring_slots) s->cfg.ring_slots = 1024;
-    if (!s->cfg.gang_arcs) s->cfg.gang_arcs = 1u << 21;
+    if (!s->cfg.gang_arcs) s->cfg.gang_arcs = 1u << 19;
     if (!s->cfg.small_vertices) s->cfg.small_vertices = 1u << 18;
     cudaGetDevice(&s->dev);
     int sms = 0, per = 0;
