@@ -38,7 +38,7 @@ L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
 # one-CTA tail kernel it hands the last levels to -- from one ncu capture of
 # the same workload (profiles/peel_persistent_rmat-s20-ef5.md); None where not
 # captured.
-NCU_TRAFFIC = {2: 45_161_472 + 4_132_096 + 7_796_480 + 0}
+NCU_TRAFFIC = {2: 45_306_624 + 3_909_632 + 7_795_712 + 0}
 
 
 def dist_env():
@@ -237,15 +237,16 @@ def reference_gpu(off, nbr, tmpdir: Path):
             "core": np.fromfile(out, dtype=np.uint32)}
 
 
-def batched_leg(args, torch, flush, with_cpu: bool, with_baseline: bool = True):
+def batched_leg(args, torch, flush, with_cpu: bool, with_baseline: bool = True, ngraphs: int | None = None):
     """The batched workload (4,096 graphs in one persistent launch): graphs/s,
     the plain one-graph-per-launch peel beside it, and the CPU bucket peel over
-    all host cores."""
+    all host cores.  ngraphs < 4,096 takes the first graphs only (the small
+    case profiled by ncu)."""
     from kcoregpu_gb300 import batch as B
     from kcoregpu_gb300 import workloads as W
     from oracle import kc_oracle as O
     t0 = time.perf_counter()
-    seg = W.batch()
+    seg = W.batch(ngraphs)
     gen_s = time.perf_counter() - t0
     G, Vt, At = seg.ngraphs, int(seg.vbase[-1]), int(seg.abase[-1])
     stream = torch.cuda.Stream()
@@ -306,6 +307,8 @@ def served_leg(requests: int, mmax: int | None, with_big: bool, rates, seed: int
     edges = [len(n) // 2 for _, n in reqs]
     srv = Server()
     srv.wait(srv.submit(*reqs[0]))   # warm-up (kernel launch, pool growth)
+    if big_pos is not None:          # and the big graph's own pool growth and first device touch
+        srv.wait(srv.submit(*reqs[big_pos]))
     rng = np.random.default_rng(seed)
     sweep = []
     for rate in list(rates) + [None]:
@@ -351,6 +354,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched leg of the default run")
+    ap.add_argument("--graphs", type=int, default=None,
+                    help="--config 4: the first N graphs of the batch only (a small case for ncu)")
     ap.add_argument("--profile", action="store_true",
                     help="device legs only (no e2e, CPU or reference-GPU legs): the command profiled by ncu")
     args = ap.parse_args()
@@ -396,8 +401,14 @@ def main():
         flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
         barrier()
         with Clocks(local) as clk:
-            bl = batched_leg(args, torch, flush, with_cpu=not args.no_cpu)
+            bl = batched_leg(args, torch, flush, with_cpu=not (args.no_cpu or args.profile),
+                             with_baseline=not args.profile, ngraphs=args.graphs)
         barrier()
+        if args.profile:
+            if rank == 0:
+                print(json.dumps({"profile_run": True, "ms_per_step": bl["ms_per_step"], "graphs": bl["graphs"],
+                                  "workload": bl["workload"]}), flush=True)
+            return
         if rank == 0:
             line = {"metric": METRIC, "value": world * bl["graphs_per_s"], "unit": "graphs/s", "n_gpus": world,
                     "steps": args.steps, "warmup": args.warmup, "ms_per_step": bl["ms_per_step"],
