@@ -17,8 +17,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) peel_batch_kernel(const __gr
         if (s >= a.ngraphs) return;
         const uint32_t g = a.schedule[s];
         const unsigned long long vb = a.vbase[g];
+        uint32_t* scratch = a.queues + (size_t)blockIdx.x * kCtaScratch * a.qcap;
         peel_graph_cta(a.offsets + vb + g, a.nbr + a.abase[g], a.core + vb, (uint32_t)(a.vbase[g + 1] - vb),
-                       a.queues + (size_t)blockIdx.x * a.qcap, a.qcap, a.err, a.kmax + g, a.levels_run + g, sh);
+                       scratch, scratch + a.qcap, a.qcap, a.err, a.kmax + g, a.levels_run + g, sh);
         __syncthreads();
     }
 }

@@ -8,6 +8,7 @@ namespace kc {
 constexpr int kBatchThreads = 512;
 constexpr int kBatchWarps = kBatchThreads / 32;
 constexpr uint32_t kBatchChunk = kBatchThreads * 2;   // queue items per walk round
+constexpr uint32_t kCtaScratch = 3;   // per-CTA scratch, in units of qcap: the queue and two alive lists
 
 struct BatchArgs {
     const unsigned long long* vbase;  // ngraphs+1: first vertex of each graph
@@ -19,7 +20,7 @@ struct BatchArgs {
     uint32_t* levels_run;             // per graph: level iterations actually run
     const uint32_t* schedule;         // graph ids in the order CTAs take them
     uint32_t* next;                   // device work-queue counter (zeroed before launch)
-    uint32_t* queues;                 // per CTA: qcap entries (peel order of its current graph)
+    uint32_t* queues;                 // per CTA: kCtaScratch*qcap entries (peel order, two alive lists)
     int* err;                         // first error (0 = ok)
     uint32_t ngraphs;
     uint32_t qcap;                    // >= max V_g

@@ -250,7 +250,7 @@ int kc_batch_upload(const kc_segcsr* s, kc_batch** out) {
     KC_B(cudaMalloc(&b->d_sched, 4 * std::max<size_t>(b->schedule.size(), 1)));
     KC_B(cudaMalloc(&b->d_next, 4));
     KC_B(cudaMalloc(&b->d_err, 4));
-    KC_B(cudaMalloc(&b->d_queues, 4 * (size_t)b->qcap * b->grid));
+    KC_B(cudaMalloc(&b->d_queues, 4 * (size_t)kCtaScratch * b->qcap * b->grid));
     KC_B(cudaMemcpyAsync(b->d_vbase, b->vbase.data(), 8 * (G + 1), cudaMemcpyHostToDevice, b->stream));
     KC_B(cudaMemcpyAsync(b->d_abase, b->abase.data(), 8 * (G + 1), cudaMemcpyHostToDevice, b->stream));
     if (offn) KC_B(cudaMemcpyAsync(b->d_off, s->offsets, 4 * offn, cudaMemcpyHostToDevice, b->stream));

@@ -18,6 +18,7 @@ struct BatchShared {
     uint32_t warp_tot[kBatchWarps];
     uint32_t qtail;                  // vertices peeled so far in this graph
     uint32_t level_start;            // qtail when the level began (set before the level's barrier)
+    uint32_t alen;                   // survivors appended to the next alive list
     uint32_t minv;                   // smallest survivor degree seen by a level's scan
     uint32_t g;                      // schedule index of the current graph
 };
@@ -41,22 +42,31 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t x, BatchShared& sh,
     return sh.warp_tot[wid] + ex;
 }
 
-// Appends the vertices v of the lanes with `pred` to the CTA's queue.
-__device__ __forceinline__ void enqueue(BatchShared& sh, uint32_t* q, bool pred, uint32_t v) {
+// Appends the vertices v of the lanes with `pred` at the position counter
+// *tail of buffer q (the CTA's queue, or an alive list).
+__device__ __forceinline__ void append_at(uint32_t* tail, uint32_t* q, bool pred, uint32_t v) {
     const unsigned m = __ballot_sync(kFull, pred);
     if (!m) return;
     const unsigned lane = threadIdx.x & 31;
     uint32_t pos = 0;
-    if (lane == 0) pos = atomicAdd(&sh.qtail, (unsigned)__popc(m));
+    if (lane == 0) pos = atomicAdd(tail, (unsigned)__popc(m));
     pos = __shfl_sync(kFull, pos, 0);
     if (pred) q[pos + __popc(m & lanemask_lt())] = v;
 }
 
+// Appends the vertices v of the lanes with `pred` to the CTA's queue.
+__device__ __forceinline__ void enqueue(BatchShared& sh, uint32_t* q, bool pred, uint32_t v) {
+    append_at(&sh.qtail, q, pred, v);
+}
+
 // Peels one graph (V vertices, graph-local CSR off/nb) with this CTA alone.
 // w (V entries) receives the core numbers, q (>= V entries) is the CTA's
-// queue / peel order.  Thread 0 writes kmax and the level iterations run.
+// queue / peel order, lists (2*qcap entries) holds two alive lists: once at
+// most half the scanned vertices survive, a level's scan appends its
+// survivors to a list and the next level scans that list instead of every
+// vertex.  Thread 0 writes kmax and the level iterations run.
 __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t* w, uint32_t V, uint32_t* q,
-                               uint32_t qcap, int* err, uint32_t* kmax_out, uint32_t* iters_out,
+                               uint32_t* lists, uint32_t qcap, int* err, uint32_t* kmax_out, uint32_t* iters_out,
                                BatchShared& sh) {
     const unsigned tid = threadIdx.x;
     if (V == 0) {   // the reference loop never runs: kmax = level-1 = 0xFFFFFFFF
@@ -84,27 +94,36 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
     __syncthreads();
 
     uint32_t level = 0, iters = 0;
+    // scan source: every vertex (src == nullptr) or the alive list src[0, nscan)
+    const uint32_t* src = nullptr;
+    uint32_t nscan = V, cur = 0;
+    bool compact = false;   // this level's scan writes the next alive list
     for (;;) {
-        if (tid == 0) { sh.minv = kFull; sh.level_start = sh.qtail; }
+        if (tid == 0) { sh.minv = kFull; sh.level_start = sh.qtail; sh.alen = 0; }
         __syncthreads();
         // a snapshot taken before the barrier: the scan below appends at once
         const uint32_t lvl_start = sh.level_start;
+        uint32_t* dst = lists + (size_t)(cur ^ 1u) * qcap;
         // scan: every vertex whose degree equals the level (ours.cc:15-25),
-        // kScanLoads independent loads in flight per thread
+        // kScanLoads independent loads in flight per thread; survivors go to
+        // the next alive list when compacting
         constexpr uint32_t kScanLoads = 8;
         uint32_t mymin = kFull;
-        for (uint32_t base = 0; base < V; base += kBatchThreads * kScanLoads) {
-            uint32_t d[kScanLoads];
+        for (uint32_t base = 0; base < nscan; base += kBatchThreads * kScanLoads) {
+            uint32_t vv[kScanLoads], d[kScanLoads];
 #pragma unroll
             for (uint32_t k = 0; k < kScanLoads; ++k) {
-                const uint32_t v = base + k * kBatchThreads + tid;
-                d[k] = v < V ? __ldcg(w + v) : kFull;
+                const uint32_t i = base + k * kBatchThreads + tid;
+                vv[k] = i < nscan ? (src ? __ldcg(src + i) : i) : kFull;
             }
 #pragma unroll
+            for (uint32_t k = 0; k < kScanLoads; ++k) d[k] = vv[k] < V ? __ldcg(w + vv[k]) : kFull;
+#pragma unroll
             for (uint32_t k = 0; k < kScanLoads; ++k) {
-                const uint32_t v = base + k * kBatchThreads + tid;
-                if (d[k] != kFull && d[k] > level) mymin = min(mymin, d[k]);
-                enqueue(sh, q, v < V && d[k] == level, v);
+                const bool surv = d[k] != kFull && d[k] > level;
+                if (surv) mymin = min(mymin, d[k]);
+                enqueue(sh, q, d[k] == level, vv[k]);
+                if (compact) append_at(&sh.alen, dst, surv, vv[k]);
             }
         }
         mymin = __reduce_min_sync(kFull, mymin);
@@ -172,6 +191,14 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
             if (tid == 0) { *kmax_out = level; *iters_out = iters; }
             return;
         }
+        // The next level scans the list this level wrote; it writes a new one
+        // once at most half of what it scans can survive.
+        if (compact) {
+            src = dst;
+            nscan = min(sh.alen, qcap);
+            cur ^= 1u;
+        }
+        compact = V - tail <= nscan / 2;
         // A level that peeled nothing changed no degree: jump to the smallest
         // survivor degree (every level in between is empty).
         uint32_t next = level + 1;

@@ -93,7 +93,7 @@ struct ServeArgs {
     uint32_t ring_cap;
     ServeCtl* ctl;
     ServeDone* done;        // device pointer of the host-mapped table
-    uint32_t* queues;       // per-CTA queue scratch for gang-1 jobs
+    uint32_t* queues;       // per-CTA scratch for gang-1 jobs (kCtaScratch*qcap entries)
     uint32_t qcap;
     uint32_t wait_us;       // bounded waits inside a gang peel
     uint32_t idle_us;       // time a CTA waits on an empty ring before it leaves
@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(kPeelThreads, 1) serve_kernel(const __grid_con
             if (bad) {
                 if (threadIdx.x == 0) sh.err = kErrInvalid;
             } else {
-                peel_graph_cta(j.off, j.nbr, j.core, j.V, s.queues + (size_t)blockIdx.x * s.qcap, s.qcap,
+                uint32_t* scratch = s.queues + (size_t)blockIdx.x * kCtaScratch * s.qcap;
+                peel_graph_cta(j.off, j.nbr, j.core, j.V, scratch, scratch + s.qcap, s.qcap,
                                &sh.err, &sh.kmax, &sh.iters, sh.u.batch);
             }
             __syncthreads();
@@ -756,7 +757,7 @@ int kc_serve_open(const kc_serve_cfg* cfg, kc_server** out) {
     if ((e = cudaHostAlloc(&s->h_done, sizeof(ServeDone) * s->cfg.ring_slots, cudaHostAllocMapped))) return fail(e, "done");
     std::memset(s->h_done, 0, sizeof(ServeDone) * s->cfg.ring_slots);
     if ((e = cudaHostGetDevicePointer(&s->d_done, s->h_done, 0))) return fail(e, "done");
-    if ((e = cudaMalloc(&s->d_queues, 4ull * s->cfg.small_vertices * s->grid))) return fail(e, "queues");
+    if ((e = cudaMalloc(&s->d_queues, 4ull * kCtaScratch * s->cfg.small_vertices * s->grid))) return fail(e, "queues");
     if ((e = cudaMallocHost(&s->h_ctl_init, sizeof(PeelCtl)))) return fail(e, "ctl init");
     std::memset(s->h_ctl_init, 0, sizeof(PeelCtl));
     for (auto& sl : s->h_ctl_init->slot) sl.min_next = 0xFFFFFFFFu;
