@@ -43,8 +43,8 @@ __device__ __forceinline__ uint32_t tail_scan(uint32_t x, TailSmem& s, uint32_t*
     __syncthreads();
     if (wid == 0) {
         uint32_t all;
-        const uint32_t te = warp_excl_scan(s.warp_tot[lane], &all);
-        s.warp_tot[lane] = te;
+        const uint32_t te = warp_excl_scan(lane < kTailWarps ? s.warp_tot[lane] : 0u, &all);
+        if (lane < kTailWarps) s.warp_tot[lane] = te;
         if (lane == 0) s.total = all;
     }
     __syncthreads();
