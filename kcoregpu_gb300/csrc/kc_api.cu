@@ -266,9 +266,24 @@ int graph_create(kc_graph** out) {
     return KC_OK;
 }
 
-int graph_load(kc_graph* g, const uint32_t* off, const uint32_t* nbr, uint32_t V) {
+// Uploads a host CSR.  With host_validate the offsets and neighbour ids are
+// checked here (an invalid graph is refused at upload); without it the
+// device checks them after the upload, before the next peel touches them
+// (kc_validate.cu), and that peel reports KC_ERR_INVALID.
+int graph_load(kc_graph* g, const uint32_t* off, const uint32_t* nbr, uint32_t V, bool host_validate = true) {
     const uint64_t E = V ? off[V] : 0;
     if (V && off[0] != 0) { set_error_msg("offsets[0] must be 0"); return KC_ERR_INVALID; }
+    if (!host_validate) {
+        int rc = reserve(g, V, E);
+        if (rc) return rc;
+        g->V = V;
+        g->E = E;
+        g->maxdeg = kFull;   // found by the device validation
+        if (V) KC_CUDA(cudaMemcpyAsync(g->d_off, off, sizeof(uint32_t) * ((size_t)V + 1), cudaMemcpyHostToDevice, g->stream));
+        if (E) KC_CUDA(cudaMemcpyAsync(g->d_nbr, nbr, sizeof(uint32_t) * E, cudaMemcpyHostToDevice, g->stream));
+        g->ran = false;
+        return KC_OK;
+    }
     uint32_t maxdeg = 0;
     for (uint32_t v = 0; v < V; ++v) {
         if (off[v + 1] < off[v]) { set_error_msg("offsets must be non-decreasing"); return KC_ERR_INVALID; }
@@ -295,6 +310,11 @@ int graph_load(kc_graph* g, const uint32_t* off, const uint32_t* nbr, uint32_t V
 int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     KC_CUDA(cudaSetDevice(g->dev));
     g->with_order = with_order;
+    const bool device_validate = g->maxdeg == kFull;
+    if (device_validate && (with_order || with_trace)) {
+        set_error_msg("peel order and trace need a graph validated at upload");
+        return KC_ERR_INVALID;
+    }
     if (g->V == 0) {   // the reference loop never runs: kmax = level-1 = 0xFFFFFFFF
         std::memset(g->h_ctl, 0, sizeof(PeelCtl));
         g->h_ctl->kmax = 0xFFFFFFFFu;
@@ -329,6 +349,11 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     if (g->epoch == 1u)
         KC_CUDA(cudaMemsetAsync(g->d_tasks, 0, sizeof(unsigned long long) * g->task_cap, g->stream));
     KC_CUDA(cudaMemcpyAsync(g->d_ctl, g->h_ctl_init, sizeof(PeelCtl), cudaMemcpyHostToDevice, g->stream));
+    KC_CUDA(cudaEventRecord(g->ev0, g->stream));
+    if (device_validate && launch_validate_csr(g->d_off, g->d_nbr, g->V, g->E, g->d_ctl, g->stream)) {
+        set_error_msg("CSR validation kernel launch failed");
+        return KC_ERR_CUDA;
+    }
     PeelArgs a;
     a.off = g->d_off;
     a.nbr = g->d_nbr;
@@ -363,7 +388,6 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         a.tail_items_cap = g->tail_items_cap;
     }
     void* args[] = {&a};
-    KC_CUDA(cudaEventRecord(g->ev0, g->stream));
     KC_CUDA(cudaLaunchCooperativeKernel(peel_kernel(), dim3(g->grid), dim3(kPeelThreads), args, 0, g->stream));
     if (tail)
         KC_CUDA(cudaLaunchKernel(tail_kernel(g->dev), dim3(1), dim3(kTailThreads), args, peel_tail_smem(), g->stream));
@@ -379,6 +403,11 @@ int graph_finish(kc_graph* g, kc_stats* st) {
     if (!g->ran) { set_error_msg("no peel has been run on this graph"); return KC_ERR_INVALID; }
     KC_CUDA(cudaStreamSynchronize(g->stream));
     g->pending = false;
+    if (g->h_ctl->err == kErrInvalid) {
+        set_error_msg("invalid CSR: offsets must start at 0 and not decrease, neighbour ids must be < V, "
+                      "degrees below 2^30");
+        return KC_ERR_INVALID;
+    }
     if (g->h_ctl->err) {
         std::string m = std::string("device peel failed at level ") + std::to_string(g->h_ctl->err_level);
         if (g->h_ctl->err == kErrCheck)
@@ -544,7 +573,7 @@ int kc_peel_csr(const uint32_t* off, const uint32_t* nbr, uint32_t V, uint32_t* 
         if (rc) return rc;
     }
     kc_graph* g = g_oneshot[dev];
-    int rc = graph_load(g, off, nbr, V);
+    int rc = graph_load(g, off, nbr, V, /*host_validate=*/false);
     if (rc) return rc;
     rc = graph_launch(g, false);
     if (rc) return rc;

@@ -165,6 +165,7 @@ int launch_single(kc_batch* b, uint32_t g) {
     KC_CUDA(cudaMemcpyAsync(b->d_gctl, b->h_gctl_init, sizeof(PeelCtl), cudaMemcpyHostToDevice, b->stream));
     PeelArgs a;
     std::memset(&a, 0, sizeof(a));
+    a.local_budget = kLocalBudget;
     a.off = b->d_off + b->vbase[g] + g;
     a.nbr = b->d_nbr + b->abase[g];
     a.w = b->d_gw;

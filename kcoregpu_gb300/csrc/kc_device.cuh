@@ -90,7 +90,8 @@ struct alignas(128) PeelCtl {
     unsigned int tail_iter;    // level iterations run before it
     unsigned int tail_items;   // fill work items of the induced CSR
     unsigned int tail_arcs;    // arcs of the induced CSR
-    unsigned int pad2[14];
+    unsigned int maxdeg;       // maximum degree found by the device-side CSR validation
+    unsigned int pad2[13];
 };
 
 struct PeelArgs {
@@ -105,7 +106,9 @@ struct PeelArgs {
     unsigned long long task_cap;
     uint32_t V;
     uint32_t shell_cap;
-    uint32_t max_level;         // max degree: no vertex survives past it
+    uint32_t max_level;         // max degree: no vertex survives past it (0xFFFFFFFF: the device
+                                // validation found it, in ctl->maxdeg; the peel returns at once
+                                // if that validation recorded an error)
     uint32_t epoch;             // 1..255, tags this run's task entries
     uint32_t wait_us;           // longest a warp waits for others before it gives up (KC_ERR_TIMEOUT)
     unsigned long long* trace;  // optional per-level timestamps (kTraceFields per level)

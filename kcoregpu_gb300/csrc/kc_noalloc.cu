@@ -125,6 +125,12 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
     noalloc_reset_ctl<<<1, 256, 0, st>>>(ctl);
     e = cudaGetLastError();
     if (e != cudaSuccess) { set_error_msg(std::string("counter reset: ") + cudaGetErrorString(e)); return KC_ERR_CUDA; }
+    // The CSR is the caller's device memory: it is checked on the device
+    // (offsets, neighbour ids, degrees) before the peel indexes with it.
+    if (launch_validate_csr(d_offsets, d_neighbors, V, n_arcs, ctl, st)) {
+        set_error_msg("kc_peel_noalloc: CSR validation launch failed");
+        return KC_ERR_CUDA;
+    }
 
     PeelArgs a;
     std::memset(&a, 0, sizeof(a));
@@ -136,7 +142,8 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
     a.ctl = ctl;
     a.task_cap = kNaTaskCap;
     a.V = V;
-    a.max_level = V;   // the max degree is below V; only a safety stop
+    a.max_level = kFull;   // from the device validation
+    a.local_budget = kLocalBudget;
     a.epoch = s.epoch;
     a.wait_us = 2000000;   // 2 s
     a.E = n_arcs;
@@ -151,6 +158,11 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
     if (e == cudaSuccess) e = cudaMemcpyAsync(&kmax, &ctl->kmax, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { set_error_msg(std::string("kc_peel_noalloc: ") + cudaGetErrorString(e)); return KC_ERR_CUDA; }
+    if (err == kErrInvalid) {
+        set_error_msg("kc_peel_noalloc: invalid CSR (offsets must start at 0 and not decrease, neighbour ids "
+                      "must be < V)");
+        return KC_ERR_INVALID;
+    }
     if (err) {
         set_error_msg("kc_peel_noalloc: device peel reported an error");
         return err;

@@ -13,4 +13,8 @@ const void* peel_persistent_fn_checked();
 // shared memory), launched after the persistent kernel on the same stream.
 const void* peel_tail_fn();
 size_t peel_tail_smem();
+// Device-side CSR validation (kc_validate.cu), stream-ordered before a peel
+// launched with max_level = 0xFFFFFFFF; returns 0 or -1 (launch error).
+int launch_validate_csr(const uint32_t* off, const uint32_t* nbr, uint32_t V, uint64_t E, PeelCtl* ctl,
+                        cudaStream_t stream);
 }  // namespace kc

@@ -881,6 +881,13 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
     const bool lead = part == 0 && threadIdx.x == 0;
     if (lead && a.shells && a.shell_cap) a.shells[0] = 0;
     uint32_t peeled_total = 0;
+    // max_level from the device-side validation that ran before this launch;
+    // nothing is peeled when it found the CSR invalid
+    uint32_t max_level = a.max_level;
+    if (max_level == kFull) {
+        if (ld_err(&ctl->err)) return;
+        max_level = ld_relaxed(&ctl->maxdeg);
+    }
 
     for (uint32_t level = 0, it = 0;; ++it) {
         w.level = level;
@@ -961,7 +968,7 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
             if (lead) { ctl->kmax = level; ctl->levels = level + 1; ctl->iterations = it + 1; }
             return;
         }
-        if (level >= a.max_level) {
+        if (level >= max_level) {
             if (lane == 0) record_error(ctl, kErrOverflow, level);
             return;
         }

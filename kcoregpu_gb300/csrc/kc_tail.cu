@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         if (tid == 0) record_error(ctl, kErrOverflow, ctl->tail_level);
         return;
     }
+    const uint32_t max_level = a.max_level == kFull ? ctl->maxdeg : a.max_level;
     const uint32_t peeled0 = ctl->tail_peeled;
     const uint32_t nquads = ctl->tail_arcs / 4;
     const uint4* nbr4 = reinterpret_cast<const uint4*>(a.tail_nbr);
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         uint32_t next = level + 1;
         const uint32_t mn = s.minv;
         if (tail == lvl_start && mn != kFull && mn > next) next = mn;
-        if (next > a.max_level) {   // cannot happen for a valid CSR: every vertex is peeled by its degree
+        if (next > max_level) {   // cannot happen for a valid CSR: every vertex is peeled by its degree
             if (tid == 0) record_error(ctl, kErrOverflow, level);
             failed = true;
             break;

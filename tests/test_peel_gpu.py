@@ -6,6 +6,7 @@ import pytest
 
 import kcoregpu_gb300 as kc
 from conftest import golden_core, golden_names, golden_serialized
+from kcoregpu_gb300 import KCoreError
 from oracle import kc_oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -145,3 +146,27 @@ def test_repeated_full_size_peels_are_stable(gpu, cfg):
     tr = g.trace()
     assert 1 <= len(tr) <= wk + 1 and int(tr[-1, 4]) == len(off) - 1
     g.free()
+
+
+def test_one_shot_peel_refuses_invalid_csr_on_the_device(gpu):
+    # kc_peel_csr checks the CSR on the device after the upload: an invalid
+    # graph is refused with KC_ERR_INVALID before the peel touches it, and the
+    # next valid call is unaffected.  (kc_graph_upload still checks at upload.)
+    off, nbr = kc.build_csr(*kc.gen_rmat(50_000, 300_000, seed=31))[:2]
+    want, wk = O.bz(off, nbr)
+    bad = nbr.copy()
+    bad[-1] = len(off) - 1 + 3
+    with pytest.raises(KCoreError) as e:
+        kc.peel_csr(off, bad)
+    assert e.value.name == "KC_ERR_INVALID"
+    dec = off.copy()
+    dec[500] = dec[499] - 1
+    with pytest.raises(KCoreError) as e:
+        kc.peel_csr(dec, nbr)
+    assert e.value.name == "KC_ERR_INVALID"
+    core, k = kc.peel_csr(off, nbr)
+    np.testing.assert_array_equal(core, want)
+    assert k == wk
+    with pytest.raises(KCoreError) as e:
+        kc.DeviceGraph(off, bad)
+    assert e.value.name == "KC_ERR_INVALID"

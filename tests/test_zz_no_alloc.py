@@ -53,3 +53,25 @@ def test_noalloc_rejects_graphs_beyond_its_limit(gpu):
     rc = lib.kc_peel_noalloc(None, None, 524288 + 1, 0, None, C.byref(kmax), None)
     assert _lib.ERRORS[rc] == "KC_ERR_INVALID"
     assert b"scratch limits" in lib.kc_last_error()
+
+
+def test_noalloc_refuses_an_invalid_csr_before_peeling(gpu):
+    # The caller's device CSR is checked on the device before the peel
+    # indexes with it: a neighbour id >= V and decreasing offsets are refused
+    # with KC_ERR_INVALID, and the next valid call works.
+    torch = pytest.importorskip("torch")
+    off, nbr = kc.build_csr(*kc.gen_er(20_000, 80_000, seed=23))[:2]
+    bad = nbr.copy()
+    bad[len(bad) // 3] = len(off) - 1 + 1
+    with pytest.raises(kc.KCoreError) as e:
+        _noalloc_peel(torch, off, bad)
+    assert e.value.name == "KC_ERR_INVALID"
+    dec = off.copy()
+    dec[100] = dec[99] - 1
+    with pytest.raises(kc.KCoreError) as e:
+        _noalloc_peel(torch, dec, nbr)
+    assert e.value.name == "KC_ERR_INVALID"
+    want, wk = kc.peel_csr(off, nbr)
+    got, gk = _noalloc_peel(torch, off, nbr)
+    np.testing.assert_array_equal(got, want)
+    assert gk == wk
