@@ -177,7 +177,8 @@ int reserve_tail(kc_graph* g, uint64_t E) {
     if (items > 0xFFFFFFFFull) { g->tail_cap_v = 0; return KC_OK; }
     if (!g->d_tail_ids) {
         KC_CUDA(cudaMalloc(&g->d_tail_ids, sizeof(uint32_t) * kTailV));
-        KC_CUDA(cudaMalloc(&g->d_tail_off, sizeof(uint32_t) * (kTailV + 1)));
+        // (kTailV + 1 offsets, rounded up to whole 16-byte words for the tail's bulk copy)
+        KC_CUDA(cudaMalloc(&g->d_tail_off, sizeof(uint32_t) * (kTailV + 4)));
         KC_CUDA(cudaMalloc(&g->d_tail_cur, sizeof(uint32_t) * kTailV));
     }
     if (cap_arcs > g->tail_cap_arcs || !g->d_tail_nbr) {

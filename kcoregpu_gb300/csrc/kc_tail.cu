@@ -23,7 +23,7 @@ constexpr int kTailQuads = 4;   // 16-byte quads per thread per walk step
 
 struct TailSmem {
     uint32_t st[kTailV];              // remaining degree; the core number once peeled
-    uint32_t off[kTailV + 1];         // induced CSR offsets (multiples of 4)
+    uint32_t off[kTailV + 4];         // induced CSR offsets (multiples of 4); the bulk copy's round-up
     uint32_t q[kTailV];               // local ids in peel order
     uint32_t pref[kTailItems + 1];    // quad prefix of the items of one walk round
     uint32_t start[kTailItems];       // first quad of each item
@@ -32,7 +32,31 @@ struct TailSmem {
     uint32_t minv;
     uint32_t total;
     uint32_t level_start;             // qtail when the level began (set before the level's barrier)
+    unsigned long long bar;           // mbarrier of the bulk copies that stage the offsets and cursors
 };
+static_assert(offsetof(TailSmem, off) % 16 == 0 && offsetof(TailSmem, st) % 16 == 0 &&
+              offsetof(TailSmem, bar) % 8 == 0, "bulk-copy destinations and the mbarrier are aligned");
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Stages `bytes` (a multiple of 16) from global `src` into shared `dst` with
+// one bulk copy (the TMA engine) that completes on mbarrier `bar`.
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
 
 // Block-wide exclusive prefix sum of one value per thread.
 __device__ __forceinline__ uint32_t tail_scan(uint32_t x, TailSmem& s, uint32_t* total) {
@@ -71,21 +95,36 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
     uint32_t it = ctl->tail_iter;
     const uint32_t it0 = it;
     const unsigned long long t_entry = now_ns();
-    {   // offsets, and degrees from the fill cursors (they stopped at offset + degree)
-        constexpr uint32_t kPer = kTailV / kTailThreads;
-        uint32_t o[kPer], c[kPer];
-#pragma unroll
-        for (uint32_t k = 0; k < kPer; ++k) {
-            const uint32_t i = tid + k * kTailThreads;
-            o[k] = i < n ? __ldcg(a.tail_off + i) : 0u;
-            c[k] = i < n ? __ldcg(a.tail_cur + i) : 0u;
+    {   // Offsets, and degrees from the fill cursors (they stopped at offset +
+        // degree): two bulk copies stage both arrays in shared memory, the
+        // cursors into the state array, which then becomes cursor - offset.
+        const uint32_t off_bytes = ((n + 1) * 4u + 15u) & ~15u;   // <= (kTailV + 4) * 4
+        const uint32_t cur_bytes = (n * 4u + 15u) & ~15u;         // <= kTailV * 4
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s.bar)) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&s.bar)),
+                         "r"(off_bytes + cur_bytes)
+                         : "memory");
+            bulk_to_smem(s.off, a.tail_off, off_bytes, &s.bar);
+            bulk_to_smem(s.st, a.tail_cur, cur_bytes, &s.bar);
         }
-#pragma unroll
-        for (uint32_t k = 0; k < kPer; ++k) {
-            const uint32_t i = tid + k * kTailThreads;
-            if (i < n) { s.off[i] = o[k]; s.st[i] = c[k] - o[k]; }
+        __syncthreads();   // the barrier is initialised before anyone polls it
+        // every thread waits for phase 0, bounded in time (the copies are
+        // 128 KB at most: a stuck wait means a broken device)
+        bool arrived = false;
+        const unsigned long long t0 = now_ns();
+        const unsigned long long limit = (unsigned long long)a.wait_us * 1000ull;
+        while (!(arrived = mbar_try_wait(&s.bar, 0)) && now_ns() - t0 < limit) {}
+        if (!__syncthreads_and(arrived)) {
+            if (tid == 0) record_error(ctl, kErrTimeout, ctl->tail_level);
+            // the copies may still land: wait for them once more, bounded, before leaving
+            const unsigned long long t1 = now_ns();
+            while (!mbar_try_wait(&s.bar, 0) && now_ns() - t1 < limit) {}
+            return;
         }
-        if (tid == 0) { s.off[n] = __ldcg(a.tail_off + n); s.qtail = 0; }
+        for (uint32_t i = tid; i < n; i += kTailThreads) s.st[i] -= s.off[i];
+        if (tid == 0) s.qtail = 0;
     }
 
     bool failed = false;
