@@ -1,5 +1,5 @@
 /*
- * kc_oracle.c - TEST INFRASTRUCTURE ONLY.  The parity checker and the timed CPU
+ * kc_oracle.c - TEST INFRASTRUCTURE ONLY.  The parity oracle and the timed CPU
  * baseline for the k-core peel.  Only tests/, __graft_entry__.smoke() and
  * bench.py's CPU legs may load this library; the product (libkcore_gb300.so)
  * never links or calls it.

@@ -59,7 +59,7 @@ def test_oracles_agree_on_random_graphs():
         assert ka == kb
 
 
-def test_checker_detects_a_planted_error():
+def test_parity_comparison_detects_a_planted_error():
     # A planted mistake lives in the oracle's output, on the CPU: the parity
     # comparison used by the GPU tests must reject it.
     off, nbr, _ = golden_serialized("two_cliques")
