@@ -166,8 +166,11 @@ int  kc_graph_device_ptrs(kc_graph* g, const uint32_t** d_offsets,
                           const uint32_t** d_neighbors, uint32_t** d_core);
 void kc_graph_free(kc_graph* g);
 
-/* One-shot: host CSR in, host core numbers out (pinned staging, cached device
- * buffers per device).  kmax as the reference computes it (0xFFFFFFFF for V=0). */
+/* One-shot: host CSR in, host core numbers out (cached device buffers per
+ * device; pinned host arrays upload fastest).  The CSR is checked on the device
+ * after the upload, before the peel reads it (KC_ERR_INVALID).  kmax as the
+ * reference computes it (0xFFFFFFFF for V=0).  Replaces kcore(Graph&),
+ * src/ours.cc:117-160, with the core numbers returned.                          */
 int  kc_peel_csr(const uint32_t* offsets, const uint32_t* neighbors, uint32_t V,
                  uint32_t* core_out, uint32_t* kmax);
 

@@ -11,16 +11,18 @@
 //  * w[v] holds deg(v) + kBias.  Bit 31 (kClaim) marks a vertex as peeled
 //    ("claimed").  A vertex is claimed exactly once, by an atomicOr that sees
 //    the bit clear, either by the frontier scan (w == level+kBias) or by the
-//    walker whose atomicSub took w from level+1 to level (ours.cc:96).  The
-//    bias keeps transient over-decrements (stale readers that are undone, as
-//    in ours.cc:102-105) from ever borrowing into the claim bit.
+//    walker whose decrement took w from level+1 to level (ours.cc:96; when
+//    the walker read level+1 before, one atomicCAS decrements and claims).
+//    The bias keeps transient over-decrements (stale readers that are undone,
+//    as in ours.cc:102-105) from ever borrowing into the claim bit.
 //  * Because claims are exclusive, the scan and the neighbour walk of one
 //    level run concurrently: scan hits are walked inline by the scanning warp,
-//    cascades go to a warp-local list, and only hubs (> kLocalArcs arcs) and
-//    list overflow go to a global queue of arc-range tasks.  There is no grid
+//    cascades go to a warp-local list while it holds at most local_budget
+//    arcs, and hubs (> kLocalArcs arcs), the rest of wide cascades and list
+//    overflow go to a global queue of arc-range tasks.  There is no grid
 //    barrier inside a level; a level ends when every CTA has finished its scan
 //    slice and every queued task is done, which the last event detects and
-//    publishes by atomicMax on `levels_done`.
+//    publishes by atomicMax on `iters_done` (level iterations completed).
 //  * Every wait is bounded in time (wait_us); on expiry the kernel records
 //    KC_ERR_TIMEOUT and returns instead of trapping.
 #pragma once
