@@ -21,8 +21,8 @@
 //    arcs, and hubs (> kLocalArcs arcs), the rest of wide cascades and list
 //    overflow go to a global queue of arc-range tasks.  There is no grid
 //    barrier inside a level; a level ends when every CTA has finished its scan
-//    slice and every queued task is done, which the last event detects and
-//    publishes by atomicMax on `iters_done` (level iterations completed).
+//    slice and every queued task is done, which every CTA reads off one
+//    packed counter of the level (LevelSlot::units_tail).
 //  * Every wait is bounded in time (wait_us); on expiry the kernel records
 //    KC_ERR_TIMEOUT and returns instead of trapping.
 #pragma once
@@ -54,15 +54,25 @@ constexpr int kErrInvalid = -8;  // malformed input found on the device (a neigh
 
 // Counters of one level iteration.  A ring of 4 slots is reused: CTA 0 clears
 // the slot of iteration i-2 when it starts iteration i, when no warp can still
-// touch it.  The 64-bit words pack a count in the high half with the vertices
-// peeled by that event in the low half, so one atomic publishes both.
+// touch it.
+//
+// Level completion.  A level's work units are the participants' scans (one
+// per CTA) and the tasks pushed to the queue.  `units_tail` packs the units
+// finished in its high half with the tasks pushed in its low half, so one
+// 64-bit word holds both sides of the test: the level is complete exactly
+// when units == participants + tasks.  A push happens inside a unit that is
+// not finished yet (a scan before its arrival, a task before its completion)
+// and is ordered before the completion of the task it pushes (the claimer
+// reads the entry written after the push), so no snapshot of the word shows
+// the equality early.  Arrivals and completions are a release fence and one
+// add; every poller sees the end from one load.
 struct alignas(128) LevelSlot {
-    unsigned int tail;  // tasks pushed in this level
-    unsigned int head;  // tasks claimed
+    unsigned long long units_tail;   // [63:32] units finished, [31:0] tasks pushed in this level
     unsigned int pad0[30];
-    unsigned long long done_peel;  // [63:32] tasks completed, [31:0] vertices they claimed
-    unsigned int pad1[30];
-    unsigned long long arr_peel;   // [63:32] CTAs arrived, [31:0] vertices their scans claimed
+    unsigned int head;               // tasks claimed
+    unsigned int pad1[31];
+    unsigned int peeled;             // vertices claimed in this level
+    unsigned int arrived;            // participants arrived (traced runs only)
     unsigned int pad2[30];
     unsigned int alive_next;  // survivors appended to the next alive list
     unsigned int min_next;    // smallest survivor state seen by the scans (0xFFFFFFFF = none)
@@ -72,7 +82,7 @@ struct alignas(128) LevelSlot {
 
 struct alignas(128) PeelCtl {
     LevelSlot slot[4];
-    unsigned int iters_done;   // atomicMax(iteration+1) when an iteration is complete
+    unsigned int iters_done;   // level iterations completed (CTA 0 writes it; diagnostics)
     unsigned int pad0[31];
     unsigned int order_tail;   // next peel-order position
     unsigned int pad1[31];

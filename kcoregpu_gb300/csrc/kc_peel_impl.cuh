@@ -84,10 +84,7 @@ __device__ __noinline__ void push_tasks(Warp& w, bool pred, uint32_t start, uint
     uint32_t ex = warp_excl_scan(nch, &tot);
     if (tot == 0) return;
     uint32_t base = 0;
-    if (lane == 0) {
-        base = atomicAdd(&w.slot->tail, tot);
-        atomicAdd(&w.a.ctl->tasks, (unsigned long long)tot);
-    }
+    if (lane == 0) base = (uint32_t)atomicAdd(&w.slot->units_tail, (unsigned long long)tot);
     base = __shfl_sync(kFull, base, 0);
     const unsigned long long first = w.task_base + base;
     if (first + tot > w.a.task_cap) {
@@ -473,11 +470,14 @@ __device__ __forceinline__ int level_state(Warp& w, uint32_t* avail) {
     int err = 0;
     if (lane == 0) {
         if (atomicCAS(&sh.poll_lock, 0u, 1u) == 0u) {
-            const unsigned ld = ld_relaxed(&w.a.ctl->iters_done);
-            const unsigned t = ld_relaxed(&w.slot->tail);
+            const unsigned long long ut = ld_relaxed64(&w.slot->units_tail);
             const unsigned h = ld_relaxed(&w.slot->head);
             const int e = ld_err(&w.a.ctl->err);
-            *(volatile unsigned*)&sh.hint_done = ld;
+            const unsigned t = (unsigned)ut;
+            // hint_done only grows: a warp of the CTA may already poll the
+            // next iteration while another still polls this one
+            if ((unsigned)(ut >> 32) == w.nparts + t && *(volatile unsigned*)&sh.hint_done < w.it + 1)
+                *(volatile unsigned*)&sh.hint_done = w.it + 1;
             *(volatile unsigned*)&sh.hint_avail = t > h ? t - h : 0u;
             *(volatile unsigned*)&sh.hint_level = w.it;
             *(volatile int*)&sh.hint_err = e;
@@ -498,27 +498,21 @@ __device__ __forceinline__ int level_state(Warp& w, uint32_t* avail) {
     return err ? -1 : 0;
 }
 
-// Announces the level complete when every CTA has arrived and every task is
-// done.  Callers have just moved one of the counters behind a full fence and
-// read the other one with an ACQUIRE load, so the tail read below cannot be
-// performed before it: tail(t2) == done(t1) with t1 < t2 proves that no task
-// was in flight at t2 (both counters only grow and done <= tail).
-__device__ __forceinline__ void maybe_complete(Warp& w, unsigned arrivals, unsigned done) {
-    const unsigned t = ld_relaxed(&w.slot->tail);
-    if (arrivals == w.nparts && t == done) {
-        atomicMax(&w.a.ctl->iters_done, w.it + 1);
-        trace(w.a, w.it, 2, now_ns());
-    }
+// Finishes `n` work units of the level (a participant's scan, or tasks).
+// The caller has fenced its writes.  Only a traced run waits for the add's
+// result, to time-stamp the event that completed the level.
+__device__ __forceinline__ void finish_units(Warp& w, uint32_t n) {
+    const unsigned long long add = (unsigned long long)n << 32;
+    const unsigned long long ut = atomicAdd(&w.slot->units_tail, add) + add;
+    if (w.a.trace && (unsigned)(ut >> 32) == w.nparts + (unsigned)ut) trace(w.a, w.it, 2, now_ns());
 }
 
-// Publishes `ndone` finished tasks.
+// Publishes `ndone` finished tasks and the vertices this warp claimed in them.
 __device__ __forceinline__ void finish_tasks(Warp& w, uint32_t ndone) {
     if (lane_id() == 0) {
-        fence_acq_rel();   // pushes and claims of these tasks before their completion
-        const unsigned long long add = ((unsigned long long)ndone << 32) | w.peeled;
-        const unsigned nd = (unsigned)((atomicAdd(&w.slot->done_peel, add) + add) >> 32);
-        __threadfence();
-        maybe_complete(w, (unsigned)(ld_acquire64(&w.slot->arr_peel) >> 32), nd);
+        if (w.peeled) atomicAdd(&w.slot->peeled, w.peeled);
+        fence_acq_rel();   // pushes, claims and the count before the completion
+        finish_units(w, ndone);
     }
     w.peeled = 0;
 }
@@ -899,7 +893,7 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         if (lead) {
             trace(a, it, 0, now_ns());
             LevelSlot* r = &ctl->slot[(it + 2) & 3];
-            r->tail = 0; r->head = 0; r->done_peel = 0; r->arr_peel = 0;
+            r->units_tail = 0; r->head = 0; r->peeled = 0; r->arrived = 0;
             r->alive_next = 0; r->min_next = kFull; r->arcs_next = 0;
             __threadfence();
         }
@@ -926,15 +920,11 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
                 atomicExch(&sh.arrive[r], 0u);
                 if (m != kFull) atomicMin(&w.slot->min_next, m);
                 if (ca) atomicAdd(&w.slot->arcs_next, ca);
+                if (p) atomicAdd(&w.slot->peeled, p);
                 __threadfence();
                 if (part == 0) trace(a, it, 1, now_ns());
-                const unsigned long long add = (1ull << 32) | p;
-                const unsigned ar = (unsigned)((atomicAdd(&w.slot->arr_peel, add) + add) >> 32);
-                if (ar == nparts) {
-                    trace(a, it, 5, now_ns());
-                    __threadfence();
-                    maybe_complete(w, ar, (unsigned)(ld_acquire64(&w.slot->done_peel) >> 32));
-                }
+                finish_units(w, 1);
+                if (a.trace && atomicAdd(&w.slot->arrived, 1u) + 1u == nparts) trace(a, it, 5, now_ns());
             }
         }
         w.peeled = 0;
@@ -946,10 +936,10 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         unsigned t = 0, an = 0, mn = 0, pi = 0;
         unsigned long long ae = 0;
         if (lane == 0) {
-            t = ld_relaxed(&w.slot->tail);
+            t = (unsigned)ld_relaxed64(&w.slot->units_tail);
             an = ld_relaxed(&w.slot->alive_next);
             mn = ld_relaxed(&w.slot->min_next);
-            pi = (unsigned)ld_relaxed64(&w.slot->arr_peel) + (unsigned)ld_relaxed64(&w.slot->done_peel);
+            pi = ld_relaxed(&w.slot->peeled);
             ae = ld_relaxed64(&w.slot->arcs_next);
         }
         t = __shfl_sync(kFull, t, 0);
@@ -960,6 +950,8 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         w.task_base += t;
         peeled_total += pi;
         if (lead) {
+            ctl->iters_done = it + 1;
+            ctl->tasks += t;
             trace(a, it, 3, now_ns());
             trace(a, it, 4, peeled_total);
             if (a.shells && level + 1 < a.shell_cap) a.shells[level + 1] = peeled_total;
