@@ -148,33 +148,51 @@ __device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u, uint
     if (__ballot_sync(kFull, glob)) push_tasks(w, glob, start, len);
 }
 
-// One neighbour u of a vertex peeled at this level (ours.cc:91-106), d its
-// state as read before: returns true when this thread's decrement took u to
-// the level and claimed it, with u's arc range in *start / *len.  When d says
-// the decrement will take u to the level, one atomicCAS decrements and claims
-// at once, and u's offsets are loaded while it is in flight: a cascade hop
-// waits for one atomic instead of a decrement, a claim and an offset load in
-// sequence.  A CAS that lost a race falls back to the reference's rule with
-// the value it saw.
-__device__ __forceinline__ bool decrement(const PeelArgs& a, uint32_t u, uint32_t d, uint32_t kk,
-                                          uint32_t* start, uint32_t* len) {
-    uint32_t* wp = a.w + u;
-    if (d == kk + 1) {
-        const uint32_t s0 = KC_LDG(a.off + u), s1 = KC_LDG(a.off + u + 1);
-        const uint32_t old = atomicCAS(wp, kk + 1, kClaim | kk);
-        if (old == kk + 1) { *start = s0; *len = s1 - s0; return true; }
-        d = old;
+// The neighbours u[j] of vertices peeled at this level (ours.cc:91-106), d[j]
+// their states as read before: f[j] is set when this thread's decrement took
+// u[j] to the level and claimed it, with u[j]'s arc range in start[j] / len[j].
+// When d says the decrement will take u to the level, one atomicCAS
+// decrements and claims at once, and u's offsets are loaded while it is in
+// flight; otherwise one atomicSub.  All four atomics are issued before any
+// result is examined, so they are in flight together.  A CAS that lost a
+// race falls back to the reference's rule with the value it saw; a
+// decrement that took u to the level claims it with atomicOr; one that found
+// u at or below the level is undone (ours.cc:102-105).
+__device__ __forceinline__ void decrement4(const PeelArgs& a, const uint32_t (&u)[4], const uint32_t (&d)[4],
+                                           uint32_t kk, bool (&f)[4], uint32_t (&start)[4], uint32_t (&len)[4]) {
+    uint32_t old[4], s0[4], s1[4];
+    unsigned cas = 0, sub = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        f[j] = false; start[j] = 0; len[j] = 0; old[j] = 0; s0[j] = 0; s1[j] = 0;
+        if (u[j] == kFull) continue;
+        if (d[j] == kk + 1) {
+            s0[j] = KC_LDG(a.off + u[j]);
+            s1[j] = KC_LDG(a.off + u[j] + 1);
+            old[j] = atomicCAS(a.w + u[j], kk + 1, kClaim | kk);
+            cas |= 1u << j;
+        } else if (d[j] > kk && d[j] < kClaim) {
+            old[j] = atomicSub(a.w + u[j], 1u);
+            sub |= 1u << j;
+        }
     }
-    if (!(d > kk && d < kClaim)) return false;
-    const uint32_t old = atomicSub(wp, 1u);
-    if (old == kk + 1) {
-        const uint32_t s0 = KC_LDG(a.off + u), s1 = KC_LDG(a.off + u + 1);
-        if (atomicOr(wp, kClaim) & kClaim) return false;
-        *start = s0; *len = s1 - s0;
-        return true;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (cas & (1u << j)) {
+            if (old[j] == kk + 1) { f[j] = true; start[j] = s0[j]; len[j] = s1[j] - s0[j]; continue; }
+            if (!(old[j] > kk && old[j] < kClaim)) continue;
+            old[j] = atomicSub(a.w + u[j], 1u);   // lost race: the plain rule with the value seen
+        } else if (!(sub & (1u << j))) {
+            continue;
+        }
+        if (old[j] == kk + 1) {
+            const uint32_t t0 = KC_LDG(a.off + u[j]), t1 = KC_LDG(a.off + u[j] + 1);
+            if (atomicOr(a.w + u[j], kClaim) & kClaim) continue;
+            f[j] = true; start[j] = t0; len[j] = t1 - t0;
+        } else if (old[j] <= kk || old[j] >= kClaim) {
+            atomicAdd(a.w + u[j], 1u);   // undo
+        }
     }
-    if (old <= kk || old >= kClaim) atomicAdd(wp, 1u);   // undo (ours.cc:102-105)
-    return false;
 }
 
 // Walks every arc of the staged items (b.start / b.pref hold first arc and
@@ -229,13 +247,8 @@ __device__ void walk_items(Warp& w) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) d[j] = (u[j] != 0xFFFFFFFFu) ? __ldcg(w.a.w + u[j]) : 0u;
         bool f[4];
-#pragma unroll
         uint32_t cs[4], cl[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            cs[j] = 0; cl[j] = 0;
-            f[j] = (u[j] != 0xFFFFFFFFu) && decrement(w.a, u[j], d[j], kk, &cs[j], &cl[j]);
-        }
+        decrement4(w.a, u, d, kk, f, cs, cl);
 #pragma unroll
         for (int j = 0; j < 4; ++j) on_claimed(w, f[j], u[j], cs[j], cl[j]);
     }
