@@ -148,57 +148,91 @@ __device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u, uint
     if (__ballot_sync(kFull, glob)) push_tasks(w, glob, start, len);
 }
 
-// The neighbours u[j] of vertices peeled at this level (ours.cc:91-106), d[j]
-// their states as read before: f[j] is set when this thread's decrement took
-// u[j] to the level and claimed it, with u[j]'s arc range in start[j] / len[j].
-// When d says the decrement will take u to the level, one atomicCAS
-// decrements and claims at once, and u's offsets are loaded while it is in
-// flight; otherwise one atomicSub.  All four atomics are issued before any
-// result is examined, so they are in flight together.  A CAS that lost a
-// race falls back to the reference's rule with the value it saw; a
-// decrement that took u to the level claims it with atomicOr; one that found
-// u at or below the level is undone (ours.cc:102-105).
-__device__ __forceinline__ void decrement4(const PeelArgs& a, const uint32_t (&u)[4], const uint32_t (&d)[4],
-                                           uint32_t kk, bool (&f)[4], uint32_t (&start)[4], uint32_t (&len)[4]) {
-    uint32_t old[4], s0[4], s1[4];
-    unsigned cas = 0, sub = 0;
+// Plain decrements issued by a walk step whose results have not been
+// examined yet (u = kFull: none).
+struct PendingDec {
+    uint32_t u[4];
+    uint32_t old[4];
+};
+
+// Examines the deferred decrements (ours.cc:96-105): one that took u to the
+// level claims it with atomicOr and walks it in this level; one that found u
+// at or below the level is undone.
+__device__ __forceinline__ void resolve_pending(Warp& w, PendingDec& pd) {
+    const uint32_t kk = w.kk;
+    unsigned race = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-        f[j] = false; start[j] = 0; len[j] = 0; old[j] = 0; s0[j] = 0; s1[j] = 0;
-        if (u[j] == kFull) continue;
-        if (d[j] == kk + 1) {
-            s0[j] = KC_LDG(a.off + u[j]);
-            s1[j] = KC_LDG(a.off + u[j] + 1);
-            old[j] = atomicCAS(a.w + u[j], kk + 1, kClaim | kk);
-            cas |= 1u << j;
-        } else if (d[j] > kk && d[j] < kClaim) {
-            old[j] = atomicSub(a.w + u[j], 1u);
-            sub |= 1u << j;
+        if (pd.u[j] == kFull) continue;
+        const uint32_t o = pd.old[j];
+        if (o == kk + 1) race |= 1u << j;
+        else if (o <= kk || o >= kClaim) atomicAdd(w.a.w + pd.u[j], 1u);   // undo
+    }
+    if (__ballot_sync(kFull, race != 0)) {
+        uint32_t t0[4], t1[4], r[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            t0[j] = 0; t1[j] = 0; r[j] = kClaim;
+            if (race & (1u << j)) {
+                t0[j] = KC_LDG(w.a.off + pd.u[j]);
+                t1[j] = KC_LDG(w.a.off + pd.u[j] + 1);
+                r[j] = atomicOr(w.a.w + pd.u[j], kClaim);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const bool f = !(r[j] & kClaim);
+            on_claimed(w, f, pd.u[j], t0[j], t1[j] - t0[j]);
         }
     }
 #pragma unroll
+    for (int j = 0; j < 4; ++j) pd.u[j] = kFull;
+}
+
+// Decrements the neighbours u[j] of vertices peeled at this level
+// (ours.cc:91-106).  A level's progress is a chain of dependent hops
+// (decrement -> claim -> walk of the claimed vertex), so a hop waits for one
+// atomic: without reading the state first, one atomicCAS(level+1 -> level |
+// claim) per neighbour decrements and claims at once, with the neighbour's
+// offsets loaded while it is in flight.  A CAS that failed returned the
+// state: a neighbour above level+1 gets a plain atomicSub whose result is
+// examined by the next step (or by the flush at the end of the walk), off
+// the hop's path; claimed neighbours and those at or below the level get
+// nothing (the reference's deg[u] > level test).  The previous step's
+// deferred decrements are resolved while these CASes are in flight.  f[j] is
+// set for the neighbours this thread claimed, with their arc ranges.
+__device__ __forceinline__ void claim_or_defer(Warp& w, const uint32_t (&u)[4], PendingDec& pd, bool (&f)[4],
+                                               uint32_t (&start)[4], uint32_t (&len)[4]) {
+    const PeelArgs& a = w.a;
+    const uint32_t kk = w.kk;
+    uint32_t old[4], s0[4], s1[4];
+#pragma unroll
     for (int j = 0; j < 4; ++j) {
-        if (cas & (1u << j)) {
-            if (old[j] == kk + 1) { f[j] = true; start[j] = s0[j]; len[j] = s1[j] - s0[j]; continue; }
-            if (!(old[j] > kk && old[j] < kClaim)) continue;
-            old[j] = atomicSub(a.w + u[j], 1u);   // lost race: the plain rule with the value seen
-        } else if (!(sub & (1u << j))) {
-            continue;
-        }
+        old[j] = kClaim; s0[j] = 0; s1[j] = 0;
+        if (u[j] == kFull) continue;
+        s0[j] = KC_LDG(a.off + u[j]);
+        s1[j] = KC_LDG(a.off + u[j] + 1);
+        old[j] = atomicCAS(a.w + u[j], kk + 1, kClaim | kk);
+    }
+    resolve_pending(w, pd);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        f[j] = false; start[j] = 0; len[j] = 0;
+        if (u[j] == kFull) continue;
         if (old[j] == kk + 1) {
-            const uint32_t t0 = KC_LDG(a.off + u[j]), t1 = KC_LDG(a.off + u[j] + 1);
-            if (atomicOr(a.w + u[j], kClaim) & kClaim) continue;
-            f[j] = true; start[j] = t0; len[j] = t1 - t0;
-        } else if (old[j] <= kk || old[j] >= kClaim) {
-            atomicAdd(a.w + u[j], 1u);   // undo
+            f[j] = true; start[j] = s0[j]; len[j] = s1[j] - s0[j];
+        } else if (old[j] > kk + 1 && old[j] < kClaim) {
+            pd.u[j] = u[j];
+            pd.old[j] = atomicSub(a.w + u[j], 1u);
         }
     }
 }
 
 // Walks every arc of the staged items (b.start / b.pref hold first arc and
 // length), lanes striding over the concatenated arcs (ours.cc:82-107); each
-// lane keeps four arcs in flight.
-__device__ void walk_items(Warp& w) {
+// lane keeps four arcs in flight.  Decrements whose results are not examined
+// yet carry over in pd to the next step.
+__device__ __forceinline__ void walk_items(Warp& w, PendingDec& pd) {
     const unsigned lane = lane_id();
     const uint32_t n = w.nitems;
     w.nitems = 0;
@@ -222,7 +256,6 @@ __device__ void walk_items(Warp& w) {
     }
     if (lane == 0) w.b.pref[n] = total;
     __syncwarp();
-    const uint32_t kk = w.kk;
     uint32_t lo = 0;
     for (uint32_t base = 0; base < total; base += 128) {
         uint32_t u[4];
@@ -243,12 +276,9 @@ __device__ void walk_items(Warp& w) {
                 }
             }
         }
-        uint32_t d[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) d[j] = (u[j] != 0xFFFFFFFFu) ? __ldcg(w.a.w + u[j]) : 0u;
         bool f[4];
         uint32_t cs[4], cl[4];
-        decrement4(w.a, u, d, kk, f, cs, cl);
+        claim_or_defer(w, u, pd, f, cs, cl);
 #pragma unroll
         for (int j = 0; j < 4; ++j) on_claimed(w, f[j], u[j], cs[j], cl[j]);
     }
@@ -258,19 +288,31 @@ __device__ void walk_items(Warp& w) {
 // Walks the staged items and then, while the cascade list is non-empty, the
 // vertices it discovered in the same level.
 __device__ void walk_with_cascades(Warp& w) {
-    walk_items(w);
+    PendingDec pd;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) { pd.u[j] = kFull; pd.old[j] = 0; }
+    walk_items(w, pd);
     const unsigned lane = lane_id();
-    while (w.nnext) {
-        const uint32_t n = w.nnext;
-        for (uint32_t i = lane; i < n; i += 32) {
-            w.b.start[i] = w.b.nstart[i];
-            w.b.pref[i] = w.b.nlen[i];
+    for (;;) {
+        while (w.nnext) {
+            const uint32_t n = w.nnext;
+            for (uint32_t i = lane; i < n; i += 32) {
+                w.b.start[i] = w.b.nstart[i];
+                w.b.pref[i] = w.b.nlen[i];
+            }
+            __syncwarp();
+            w.nnext = 0;
+            w.narcs = 0;
+            w.nitems = n;
+            walk_items(w, pd);
         }
-        __syncwarp();
-        w.nnext = 0;
-        w.narcs = 0;
-        w.nitems = n;
-        walk_items(w);
+        // the deferred decrements of the last steps; a raced claim among
+        // them starts another cascade
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) any |= pd.u[j] != kFull;
+        if (!__any_sync(kFull, any)) break;
+        resolve_pending(w, pd);
     }
 }
 
