@@ -316,10 +316,11 @@ __device__ void walk_with_cascades(Warp& w) {
     }
 }
 
-// Stages the claimed vertices v[j] (mask bits, up to 4 per lane) as walk
-// items; hubs go to the task queue.  Flushes the batch first when it could
-// overflow.
-__device__ __forceinline__ void stage_claims(Warp& w, const uint32_t (&v)[4], unsigned mine) {
+// Stages the claimed vertices v[j] (mask bits, up to 4 per lane; arcs
+// [s0[j], s1[j])) as walk items; hubs go to the task queue.  Flushes the
+// batch first when it could overflow.
+__device__ __forceinline__ void stage_claims(Warp& w, const uint32_t (&v)[4], unsigned mine, const uint32_t (&s0)[4],
+                                             const uint32_t (&s1)[4]) {
     uint32_t st[4], ln[4];
     unsigned localm = 0, hubm = 0;
 #pragma unroll
@@ -327,8 +328,8 @@ __device__ __forceinline__ void stage_claims(Warp& w, const uint32_t (&v)[4], un
         st[j] = 0; ln[j] = 0;
         if (mine & (1u << j)) {
             if (!IN(v[j], w.a.V, 8)) continue;
-            st[j] = KC_LDG(w.a.off + v[j]);
-            ln[j] = KC_LDG(w.a.off + v[j] + 1) - st[j];
+            st[j] = s0[j];
+            ln[j] = s1[j] - s0[j];
             if (ln[j] == 0) continue;
             if (ln[j] <= kLocalArcs) localm |= 1u << j; else hubm |= 1u << j;
         }
@@ -372,13 +373,21 @@ __device__ __forceinline__ void append_survivors(Warp& w, const uint32_t (&v)[4]
         if ((surv & (1u << j)) && IN(base, w.a.V, 9)) out[base++] = v[j];
 }
 
-// Claims (atomicOr) the hit vertices v[j]; returns the mask of those this
-// lane claimed, recording their core number.
-__device__ __forceinline__ unsigned claim_hits(Warp& w, const uint32_t (&v)[4], unsigned hit) {
+// Claims (atomicOr) the hit vertices v[j], their offsets s0/s1 loaded while
+// the atomics are in flight; returns the mask of those this lane claimed,
+// recording their core number.
+__device__ __forceinline__ unsigned claim_hits(Warp& w, const uint32_t (&v)[4], unsigned hit, uint32_t (&s0)[4],
+                                               uint32_t (&s1)[4]) {
     unsigned o[4] = {kClaim, kClaim, kClaim, kClaim};
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
-        if ((hit & (1u << j)) && IN(v[j], w.a.V, 10)) o[j] = atomicOr(w.a.w + v[j], kClaim);
+    for (int j = 0; j < 4; ++j) {
+        s0[j] = 0; s1[j] = 0;
+        if ((hit & (1u << j)) && IN(v[j], w.a.V, 10)) {
+            s0[j] = KC_LDG(w.a.off + v[j]);
+            s1[j] = KC_LDG(w.a.off + v[j] + 1);
+            o[j] = atomicOr(w.a.w + v[j], kClaim);
+        }
+    }
     unsigned mine = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
@@ -388,7 +397,8 @@ __device__ __forceinline__ unsigned claim_hits(Warp& w, const uint32_t (&v)[4], 
 
 // Common tail of one scan step: publishes claims (peel order, count) and
 // stages their walk.
-__device__ __forceinline__ void after_claims(Warp& w, const uint32_t (&v)[4], unsigned mine) {
+__device__ __forceinline__ void after_claims(Warp& w, const uint32_t (&v)[4], unsigned mine, const uint32_t (&s0)[4],
+                                             const uint32_t (&s1)[4]) {
     const unsigned lane = lane_id();
     uint32_t tot;
     const uint32_t ex = warp_excl_scan(__popc(mine), &tot);
@@ -402,7 +412,7 @@ __device__ __forceinline__ void after_claims(Warp& w, const uint32_t (&v)[4], un
         for (int j = 0; j < 4; ++j)
             if ((mine & (1u << j)) && IN(pos, w.a.V, 12)) w.a.order[pos++] = v[j];
     }
-    if (w.level > 0) stage_claims(w, v, mine);
+    if (w.level > 0) stage_claims(w, v, mine, s0, s1);
 }
 
 // Scan of this warp's share of the vertices for level w.level (ours.cc:15-25):
@@ -450,7 +460,9 @@ __device__ void scan_level(Warp& w, uint32_t gw) {
             }
             if (compact) append_survivors(w, v, surv);
             if (!__ballot_sync(kFull, hit != 0)) continue;
-            after_claims(w, v, claim_hits(w, v, hit));
+            uint32_t s0[4], s1[4];
+            const unsigned mine = claim_hits(w, v, hit, s0, s1);
+            after_claims(w, v, mine, s0, s1);
         }
     } else {
         const uint32_t ngroups = (a.V + 127) / 128;
@@ -478,7 +490,11 @@ __device__ void scan_level(Warp& w, uint32_t gw) {
                     if (xs[j] > kk && xs[j] < kClaim) { surv |= 1u << j; w.minv = min(w.minv, xs[j]); w.arcs += xs[j] - kBias; }
                 }
                 if (compact) append_survivors(w, v, surv);
-                if (__ballot_sync(kFull, hit != 0)) after_claims(w, v, claim_hits(w, v, hit));
+                if (__ballot_sync(kFull, hit != 0)) {
+                    uint32_t s0[4], s1[4];
+                    const unsigned mine = claim_hits(w, v, hit, s0, s1);
+                    after_claims(w, v, mine, s0, s1);
+                }
             }
         }
         for (uint32_t g = gw; w.level == 0 && g < ngroups; g += w.nwt) {
@@ -506,7 +522,8 @@ __device__ void scan_level(Warp& w, uint32_t gw) {
                 for (int j = 0; j < 4; ++j)
                     if (!(st[j] & kClaim)) { surv |= 1u << j; w.minv = min(w.minv, st[j]); w.arcs += st[j] - kBias; }
                 if (compact) append_survivors(w, v, surv);
-                after_claims(w, v, mine);
+                const uint32_t none[4] = {0u, 0u, 0u, 0u};   // level 0 stages no walk
+                after_claims(w, v, mine, none, none);
             }
         }
     }
