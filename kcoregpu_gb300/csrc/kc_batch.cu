@@ -9,6 +9,7 @@ namespace {
 
 __global__ void __launch_bounds__(kBatchThreads, 2) peel_batch_kernel(const __grid_constant__ BatchArgs a) {
     __shared__ BatchShared sh;
+    extern __shared__ uint32_t peeled_bits[];   // (bits_cap + 31) / 32 words
     for (;;) {
         if (threadIdx.x == 0) sh.g = atomicAdd(a.next, 1u);
         __syncthreads();
@@ -19,7 +20,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) peel_batch_kernel(const __gr
         const unsigned long long vb = a.vbase[g];
         uint32_t* scratch = a.queues + (size_t)blockIdx.x * kCtaScratch * a.qcap;
         peel_graph_cta(a.offsets + vb + g, a.nbr + a.abase[g], a.core + vb, (uint32_t)(a.vbase[g + 1] - vb),
-                       scratch, scratch + a.qcap, a.qcap, a.err, a.kmax + g, a.levels_run + g, sh);
+                       scratch, scratch + a.qcap, a.qcap, a.err, a.kmax + g, a.levels_run + g, sh,
+                       a.bits_cap ? peeled_bits : nullptr, a.bits_cap);
         __syncthreads();
     }
 }

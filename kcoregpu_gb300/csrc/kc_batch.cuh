@@ -9,6 +9,9 @@ constexpr int kBatchThreads = 512;
 constexpr int kBatchWarps = kBatchThreads / 32;
 constexpr uint32_t kBatchChunk = kBatchThreads * 2;   // queue items per walk round
 constexpr uint32_t kCtaScratch = 3;   // per-CTA scratch, in units of qcap: the queue and two alive lists
+// Largest graph (vertices) whose peeled-vertex bitmap the batched kernel keeps
+// in shared memory: 96 KB, so two CTAs still fit on one SM.
+constexpr uint32_t kBatchBitsMax = 96u * 1024u * 8u;
 
 struct BatchArgs {
     const unsigned long long* vbase;  // ngraphs+1: first vertex of each graph
@@ -24,6 +27,7 @@ struct BatchArgs {
     int* err;                         // first error (0 = ok)
     uint32_t ngraphs;
     uint32_t qcap;                    // >= max V_g
+    uint32_t bits_cap;                // vertices the dynamic shared-memory bitmap covers (0 = none)
 };
 
 const void* peel_batch_fn();

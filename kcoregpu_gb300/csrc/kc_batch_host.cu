@@ -46,6 +46,8 @@ struct kc_batch {
     std::vector<uint32_t> giants;     // graphs run with the grid-wide peel instead
     uint32_t qcap = 0;                // queue entries per CTA (max V of the batched graphs)
     int grid = 0;                     // CTAs of the batched kernel
+    uint32_t bits_cap = 0;            // vertices of the per-CTA peeled bitmap (shared memory)
+    size_t bits_bytes = 0;            // its dynamic shared memory
     // device
     unsigned long long *d_vbase = nullptr, *d_abase = nullptr;
     uint32_t *d_off = nullptr, *d_nbr = nullptr, *d_core = nullptr, *d_kmax = nullptr, *d_levels = nullptr;
@@ -230,7 +232,14 @@ int kc_batch_upload(const kc_segcsr* s, kc_batch** out) {
     cudaGetDevice(&b->dev);
     int sms = 0, per = 0, gper = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_batch_fn(), kBatchThreads, 0);
+    // the peeled-vertex bitmap covers the largest graph, up to kBatchBitsMax
+    uint32_t vmax = 0;
+    for (const auto& p : b->plan) vmax = std::max(vmax, p.V);
+    b->bits_cap = std::min(vmax, kBatchBitsMax);
+    b->bits_bytes = (size_t)((b->bits_cap + 31) / 32) * 4;
+    if (b->bits_bytes > 48 * 1024)
+        cudaFuncSetAttribute(peel_batch_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->bits_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_batch_fn(), kBatchThreads, b->bits_bytes);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gper, peel_persistent_fn(), kPeelThreads, 0);
     b->ggrid = gper > 0 ? sms : 0;   // giants: one CTA per SM, as the single-graph peel
     autotune(b, sms, std::max(1, per));
@@ -305,8 +314,9 @@ int kc_batch_peel_async(kc_batch* b) {
         a.err = b->d_err;
         a.ngraphs = (uint32_t)b->schedule.size();
         a.qcap = b->qcap;
+        a.bits_cap = b->bits_cap;
         void* args[] = {&a};
-        KC_CUDA(cudaLaunchKernel(peel_batch_fn(), dim3(b->grid), dim3(kBatchThreads), args, 0, b->stream));
+        KC_CUDA(cudaLaunchKernel(peel_batch_fn(), dim3(b->grid), dim3(kBatchThreads), args, b->bits_bytes, b->stream));
     }
     KC_CUDA(cudaEventRecord(b->ev1, b->stream));
     return KC_OK;

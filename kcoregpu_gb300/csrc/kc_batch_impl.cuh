@@ -59,15 +59,27 @@ __device__ __forceinline__ void enqueue(BatchShared& sh, uint32_t* q, bool pred,
     append_at(&sh.qtail, q, pred, v);
 }
 
+// Sets bit v of the shared-memory bitmap for the lanes with `pred`.
+__device__ __forceinline__ void mark_peeled(uint32_t* bits, bool pred, uint32_t v) {
+    if (pred) atomicOr(bits + (v >> 5), 1u << (v & 31u));
+}
+
 // Peels one graph (V vertices, graph-local CSR off/nb) with this CTA alone.
 // w (V entries) receives the core numbers, q (>= V entries) is the CTA's
 // queue / peel order, lists (2*qcap entries) holds two alive lists: once at
 // most half the scanned vertices survive, a level's scan appends its
 // survivors to a list and the next level scans that list instead of every
 // vertex.  Thread 0 writes kmax and the level iterations run.
+//
+// bits (shared memory, bits_cap vertices, or null): a bitmap of the vertices
+// queued so far.  With it the walk tests a neighbour's bit instead of reading
+// its state from L2 first: an arc to a peeled vertex costs no L2 request, an
+// arc to a live one costs one atomicSub, whose result decides as the
+// reference's rule does (ours.cc:91-106; a neighbour queued by another thread
+// of the same round whose bit was not yet visible is decremented and undone).
 __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t* w, uint32_t V, uint32_t* q,
                                uint32_t* lists, uint32_t qcap, int* err, uint32_t* kmax_out, uint32_t* iters_out,
-                               BatchShared& sh) {
+                               BatchShared& sh, uint32_t* bits = nullptr, uint32_t bits_cap = 0) {
     const unsigned tid = threadIdx.x;
     if (V == 0) {   // the reference loop never runs: kmax = level-1 = 0xFFFFFFFF
         if (tid == 0) { *kmax_out = 0xFFFFFFFFu; *iters_out = 0; }
@@ -90,6 +102,9 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
             if (v < V) w[v] = o[k];
         }
     }
+    const bool use_bits = bits != nullptr && V <= bits_cap;
+    if (use_bits)
+        for (uint32_t i = tid; i < (V + 31) / 32; i += kBatchThreads) bits[i] = 0u;
     if (tid == 0) sh.qtail = 0;
     __syncthreads();
 
@@ -123,6 +138,7 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
                 const bool surv = d[k] != kFull && d[k] > level;
                 if (surv) mymin = min(mymin, d[k]);
                 enqueue(sh, q, d[k] == level, vv[k]);
+                if (use_bits) mark_peeled(bits, d[k] == level, vv[k]);
                 if (compact) append_at(&sh.alen, dst, surv, vv[k]);
             }
         }
@@ -166,19 +182,31 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
                         u[j] = KC_LDG(nb + sh.start[lo] + (arc - sh.pref[lo]));
                     }
                 }
-                uint32_t d[kWalkArcs];
+                // live: the reference's deg[u] > level test, from the bitmap or
+                // from a read of the state
+                bool live[kWalkArcs];
+                if (use_bits) {
 #pragma unroll
-                for (int j = 0; j < kWalkArcs; ++j) d[j] = u[j] < V ? __ldcg(w + u[j]) : 0u;
+                    for (int j = 0; j < kWalkArcs; ++j)
+                        live[j] = u[j] < V && !((bits[u[j] >> 5] >> (u[j] & 31u)) & 1u);
+                } else {
+                    uint32_t d[kWalkArcs];
+#pragma unroll
+                    for (int j = 0; j < kWalkArcs; ++j) d[j] = u[j] < V ? __ldcg(w + u[j]) : 0u;
+#pragma unroll
+                    for (int j = 0; j < kWalkArcs; ++j) live[j] = u[j] < V && d[j] > level;
+                }
                 uint32_t old[kWalkArcs];
 #pragma unroll
-                for (int j = 0; j < kWalkArcs; ++j) old[j] = (u[j] < V && d[j] > level) ? atomicSub(w + u[j], 1u) : 0u;
+                for (int j = 0; j < kWalkArcs; ++j) old[j] = live[j] ? atomicSub(w + u[j], 1u) : 0u;
 #pragma unroll
                 for (int j = 0; j < kWalkArcs; ++j) {
                     // (ours.cc:91-106): the decrement that took u to the level
                     // queues it; one that raced below the level is undone
-                    const bool live = u[j] < V && d[j] > level;
-                    if (live && old[j] <= level) atomicAdd(w + u[j], 1u);
-                    enqueue(sh, q, live && old[j] == level + 1, u[j]);
+                    if (live[j] && old[j] <= level) atomicAdd(w + u[j], 1u);
+                    const bool hit = live[j] && old[j] == level + 1;
+                    if (use_bits) mark_peeled(bits, hit, u[j]);
+                    enqueue(sh, q, hit, u[j]);
                 }
             }
             __syncthreads();
