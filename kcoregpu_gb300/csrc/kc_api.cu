@@ -151,6 +151,17 @@ void tail_limits(uint32_t* cap_v, uint32_t* cap_arcs) {
     *cap_arcs = arcs;
 }
 
+// Walk mode of the one-graph peel: claim by CAS without reading the state
+// first (KC_CLAIM_CAS, default 1).
+uint32_t claim_cas() {
+    static uint32_t c = 1;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (const char* e = std::getenv("KC_CLAIM_CAS")) c = std::atoi(e) != 0 ? 1u : 0u;
+    });
+    return c;
+}
+
 // Arcs a warp's cascade list may hold before the rest of a cascade is queued
 // for other warps (KC_LOCAL_BUDGET, default kLocalBudget).
 uint32_t local_budget() {
@@ -377,6 +388,7 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     a.trace = with_trace ? g->d_trace : nullptr;
     a.trace_cap = with_trace ? g->trace_cap : 0;
     a.local_budget = local_budget();
+    a.claim_cas = claim_cas();
     const bool tail = g->tail_cap_v != 0;
     if (tail) {
         a.tail_cap_v = g->tail_cap_v;

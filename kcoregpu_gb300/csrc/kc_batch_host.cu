@@ -168,6 +168,7 @@ int launch_single(kc_batch* b, uint32_t g) {
     PeelArgs a;
     std::memset(&a, 0, sizeof(a));
     a.local_budget = kLocalBudget;
+    a.claim_cas = 1;   // one giant graph on the whole GPU
     a.off = b->d_off + b->vbase[g] + g;
     a.nbr = b->d_nbr + b->abase[g];
     a.w = b->d_gw;
@@ -237,8 +238,8 @@ int kc_batch_upload(const kc_segcsr* s, kc_batch** out) {
     for (const auto& p : b->plan) vmax = std::max(vmax, p.V);
     b->bits_cap = std::min(vmax, kBatchBitsMax);
     b->bits_bytes = (size_t)((b->bits_cap + 31) / 32) * 4;
-    if (b->bits_bytes > 48 * 1024)
-        cudaFuncSetAttribute(peel_batch_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->bits_bytes);
+    // static plus dynamic shared memory may exceed the default 48 KB window
+    cudaFuncSetAttribute(peel_batch_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->bits_bytes);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_batch_fn(), kBatchThreads, b->bits_bytes);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gper, peel_persistent_fn(), kPeelThreads, 0);
     b->ggrid = gper > 0 ? sms : 0;   // giants: one CTA per SM, as the single-graph peel

@@ -143,6 +143,9 @@ struct PeelArgs {
     unsigned long long* tail_items = nullptr;  // fill work items: local id << 32 | arc chunk
     uint32_t tail_items_cap = 0;
     uint32_t local_budget = kLocalBudget;      // arcs a warp's cascade list may hold
+    uint32_t claim_cas = 0;     // 1: the walk claims by CAS without reading the state first (one graph on
+                                // the whole GPU: latency-bound); 0: it reads the state first (fewer atomics,
+                                // for kernels that peel many graphs at once)
 };
 
 // Tail peel: one CTA of kTailThreads threads, states in shared memory.

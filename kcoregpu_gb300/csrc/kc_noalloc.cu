@@ -144,6 +144,7 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
     a.V = V;
     a.max_level = kFull;   // from the device validation
     a.local_budget = kLocalBudget;
+    a.claim_cas = 1;   // one graph on the whole GPU
     a.epoch = s.epoch;
     a.wait_us = 2000000;   // 2 s
     a.E = n_arcs;

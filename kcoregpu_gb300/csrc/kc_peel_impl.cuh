@@ -148,6 +148,53 @@ __device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u, uint
     if (__ballot_sync(kFull, glob)) push_tasks(w, glob, start, len);
 }
 
+// The neighbours u[j] of vertices peeled at this level (ours.cc:91-106), d[j]
+// their states as read before: f[j] is set when this thread's decrement took
+// u[j] to the level and claimed it, with u[j]'s arc range in start[j] / len[j].
+// When d says the decrement will take u to the level, one atomicCAS
+// decrements and claims at once, and u's offsets are loaded while it is in
+// flight; otherwise one atomicSub.  All four atomics are issued before any
+// result is examined, so they are in flight together.  A CAS that lost a
+// race falls back to the reference's rule with the value it saw; a
+// decrement that took u to the level claims it with atomicOr; one that found
+// u at or below the level is undone (ours.cc:102-105).
+__device__ __forceinline__ void decrement4(const PeelArgs& a, const uint32_t (&u)[4], const uint32_t (&d)[4],
+                                           uint32_t kk, bool (&f)[4], uint32_t (&start)[4], uint32_t (&len)[4]) {
+    uint32_t old[4], s0[4], s1[4];
+    unsigned cas = 0, sub = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        f[j] = false; start[j] = 0; len[j] = 0; old[j] = 0; s0[j] = 0; s1[j] = 0;
+        if (u[j] == kFull) continue;
+        if (d[j] == kk + 1) {
+            s0[j] = KC_LDG(a.off + u[j]);
+            s1[j] = KC_LDG(a.off + u[j] + 1);
+            old[j] = atomicCAS(a.w + u[j], kk + 1, kClaim | kk);
+            cas |= 1u << j;
+        } else if (d[j] > kk && d[j] < kClaim) {
+            old[j] = atomicSub(a.w + u[j], 1u);
+            sub |= 1u << j;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (cas & (1u << j)) {
+            if (old[j] == kk + 1) { f[j] = true; start[j] = s0[j]; len[j] = s1[j] - s0[j]; continue; }
+            if (!(old[j] > kk && old[j] < kClaim)) continue;
+            old[j] = atomicSub(a.w + u[j], 1u);   // lost race: the plain rule with the value seen
+        } else if (!(sub & (1u << j))) {
+            continue;
+        }
+        if (old[j] == kk + 1) {
+            const uint32_t t0 = KC_LDG(a.off + u[j]), t1 = KC_LDG(a.off + u[j] + 1);
+            if (atomicOr(a.w + u[j], kClaim) & kClaim) continue;
+            f[j] = true; start[j] = t0; len[j] = t1 - t0;
+        } else if (old[j] <= kk || old[j] >= kClaim) {
+            atomicAdd(a.w + u[j], 1u);   // undo
+        }
+    }
+}
+
 // Plain decrements issued by a walk step whose results have not been
 // examined yet (u = kFull: none).
 struct PendingDec {
@@ -230,8 +277,9 @@ __device__ __forceinline__ void claim_or_defer(Warp& w, const uint32_t (&u)[4], 
 
 // Walks every arc of the staged items (b.start / b.pref hold first arc and
 // length), lanes striding over the concatenated arcs (ours.cc:82-107); each
-// lane keeps four arcs in flight.  Decrements whose results are not examined
-// yet carry over in pd to the next step.
+// lane keeps four arcs in flight.  With claim_cas, decrements whose results
+// are not examined yet carry over in pd to the next step; without, each
+// step reads the neighbours' states first and settles its decrements.
 __device__ __forceinline__ void walk_items(Warp& w, PendingDec& pd) {
     const unsigned lane = lane_id();
     const uint32_t n = w.nitems;
@@ -278,7 +326,14 @@ __device__ __forceinline__ void walk_items(Warp& w, PendingDec& pd) {
         }
         bool f[4];
         uint32_t cs[4], cl[4];
-        claim_or_defer(w, u, pd, f, cs, cl);
+        if (w.a.claim_cas) {
+            claim_or_defer(w, u, pd, f, cs, cl);
+        } else {
+            uint32_t d[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) d[j] = (u[j] != kFull) ? __ldcg(w.a.w + u[j]) : 0u;
+            decrement4(w.a, u, d, w.kk, f, cs, cl);
+        }
 #pragma unroll
         for (int j = 0; j < 4; ++j) on_claimed(w, f[j], u[j], cs[j], cl[j]);
     }

@@ -95,6 +95,7 @@ struct ServeArgs {
     ServeDone* done;        // device pointer of the host-mapped table
     uint32_t* queues;       // per-CTA scratch for gang-1 jobs (kCtaScratch*qcap entries)
     uint32_t qcap;
+    uint32_t bits_cap;      // vertices of the peeled bitmap of gang-1 jobs (dynamic shared memory)
     uint32_t wait_us;       // bounded waits inside a gang peel
     uint32_t idle_us;       // time a CTA waits on an empty ring before it leaves
     unsigned long long cursor0;   // oldest unfinished job when the kernel was launched
@@ -189,6 +190,7 @@ __device__ void publish_done(const ServeArgs& s, const ServeJob& j, uint32_t kma
 }
 
 __global__ void __launch_bounds__(kPeelThreads, 1) serve_kernel(const __grid_constant__ ServeArgs s) {
+    extern __shared__ uint32_t serve_bits[];   // (bits_cap + 31) / 32 words
     __shared__ ServeShared sh;
     unsigned long long cursor = s.cursor0;   // ring position: jobs before it end below this CTA's tickets
     for (;;) {
@@ -237,7 +239,8 @@ __global__ void __launch_bounds__(kPeelThreads, 1) serve_kernel(const __grid_con
             } else {
                 uint32_t* scratch = s.queues + (size_t)blockIdx.x * kCtaScratch * s.qcap;
                 peel_graph_cta(j.off, j.nbr, j.core, j.V, scratch, scratch + s.qcap, s.qcap,
-                               &sh.err, &sh.kmax, &sh.iters, sh.u.batch);
+                               &sh.err, &sh.kmax, &sh.iters, sh.u.batch, s.bits_cap ? serve_bits : nullptr,
+                               s.bits_cap);
             }
             __syncthreads();
             if (threadIdx.x == 0) dn->t_peeled = now_ns();
@@ -347,6 +350,8 @@ struct kc_server {
     kc_serve_cfg cfg{};
     int dev = 0;
     int grid = 0;
+    uint32_t bits_cap = 0;   // vertices of the gang-1 jobs' peeled bitmap
+    size_t bits_bytes = 0;   // its dynamic shared memory per CTA
     cudaStream_t ks = nullptr;     // serve kernel
     cudaStream_t cs = nullptr;     // copies, allocations, publication
     ServeCtl* d_ctl = nullptr;
@@ -511,6 +516,7 @@ int launch_kernel(kc_server* s) {
     a.done = s->d_done;
     a.queues = s->d_queues;
     a.qcap = s->cfg.small_vertices;
+    a.bits_cap = s->bits_cap;
     a.wait_us = 2000000;    // 2 s
     a.idle_us = 10000000;   // 10 s safety net: the request loop stops an idle kernel after 100 ms itself
     // ring position where the new kernel's CTAs start looking: the oldest job
@@ -521,7 +527,8 @@ int launch_kernel(kc_server* s) {
         if (r->state == 2) c0 = std::min(c0, r->seq);
     a.cursor0 = c0;
     void* args[] = {&a};
-    KC_CUDA(cudaLaunchCooperativeKernel((const void*)serve_kernel, dim3(s->grid), dim3(kPeelThreads), args, 0, s->ks));
+    KC_CUDA(cudaLaunchCooperativeKernel((const void*)serve_kernel, dim3(s->grid), dim3(kPeelThreads), args, s->bits_bytes,
+                                        s->ks));
     s->kernel_running = true;
     return KC_OK;
 }
@@ -734,7 +741,13 @@ int kc_serve_open(const kc_serve_cfg* cfg, kc_server** out) {
     cudaGetDevice(&s->dev);
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)serve_kernel, kPeelThreads, 0);
+    // gang-1 jobs (at most small_vertices vertices) keep a bitmap of their
+    // queued vertices in shared memory, up to kBatchBitsMax vertices
+    s->bits_cap = std::min(s->cfg.small_vertices, kBatchBitsMax);
+    s->bits_bytes = (size_t)((s->bits_cap + 31) / 32) * 4;
+    // static plus dynamic shared memory exceeds the default 48 KB window
+    cudaFuncSetAttribute((const void*)serve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->bits_bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)serve_kernel, kPeelThreads, s->bits_bytes);
     s->grid = sms * std::max(1, per);
     if (!s->cfg.max_gang || s->cfg.max_gang > (uint32_t)s->grid) s->cfg.max_gang = (uint32_t)s->grid;
     int pageable = 0;
