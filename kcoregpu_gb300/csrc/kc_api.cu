@@ -134,14 +134,14 @@ void release(kc_graph* g) {
 
 uint64_t task_capacity(uint32_t V, uint64_t E) { return (uint64_t)V + E / kChunk + 64; }
 
-// Tail hand-off limits: at most KC_TAIL_V survivors (default and maximum
-// kTailV; 0 turns the hand-off off) whose induced arcs fit KC_TAIL_ARCS
-// (default kTailArcs).
+// Tail hand-off limits: at most KC_TAIL_V survivors (default kTailHandoffV,
+// maximum kTailV; 0 turns the hand-off off) whose induced arcs fit
+// KC_TAIL_ARCS (default kTailArcs).
 void tail_limits(uint32_t* cap_v, uint32_t* cap_arcs) {
     static uint32_t v = 0, arcs = 0;
     static std::once_flag once;
     std::call_once(once, [] {
-        v = kTailV;
+        v = kTailHandoffV;
         arcs = kTailArcs;
         if (const char* e = std::getenv("KC_TAIL_V")) v = (uint32_t)std::min<long long>(std::max(0ll, std::atoll(e)), kTailV);
         if (const char* e = std::getenv("KC_TAIL_ARCS"))

@@ -152,6 +152,8 @@ struct PeelArgs {
 constexpr uint32_t kTailThreads = 1024;
 constexpr uint32_t kTailWarps = kTailThreads / 32;
 constexpr uint32_t kTailV = 16384;        // largest tail (shared-memory states)
+constexpr uint32_t kTailHandoffV = 12288;  // default hand-off point (survivors); measured best of
+                                           // 8,192 / 12,288 / 16,384 on the three single-graph workloads
 constexpr uint32_t kTailItems = 2 * kTailThreads;   // queue entries walked per round (2 per thread)
 constexpr uint32_t kTailArcs = 1u << 22;  // default largest induced CSR handed over
 constexpr uint32_t kFillChunk = 256;      // raw arcs per fill work item
