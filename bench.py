@@ -237,6 +237,44 @@ def reference_gpu(off, nbr, tmpdir: Path):
             "core": np.fromfile(out, dtype=np.uint32)}
 
 
+def e2e_leg(args, kc, V: int, arcs: int, off, nbr, want, flush, torch) -> float:
+    """End to end through the public one-shot call (kc_peel_csr): pinned H2D of
+    the CSR, the device-side CSR check, the peel and D2H of the core numbers,
+    every step; returns the mean seconds per call."""
+    lib = kc.lib()
+    h_off = lib.kc_host_alloc(4 * (V + 1))
+    h_nbr = lib.kc_host_alloc(4 * max(arcs, 1))
+    h_core = lib.kc_host_alloc(4 * max(V, 1))
+    a_off = np.ctypeslib.as_array(C.cast(h_off, C.POINTER(C.c_uint32)), shape=(V + 1,))
+    a_nbr = np.ctypeslib.as_array(C.cast(h_nbr, C.POINTER(C.c_uint32)), shape=(max(arcs, 1),))
+    a_off[:] = off
+    a_nbr[:arcs] = nbr
+    u32p = C.POINTER(C.c_uint32)
+    kout = C.c_uint32()
+
+    def e2e_call():
+        rc = lib.kc_peel_csr(C.cast(h_off, u32p), C.cast(h_nbr, u32p), V, C.cast(h_core, u32p), C.byref(kout))
+        if rc:
+            raise SystemExit(f"kc_peel_csr failed: {rc}")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_call()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_call()
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / len(e2e_t)
+    got = np.ctypeslib.as_array(C.cast(h_core, u32p), shape=(V,))
+    if not np.array_equal(got, want):
+        raise SystemExit("bench: e2e core numbers differ from the oracle")
+    for p in (h_off, h_nbr, h_core):
+        lib.kc_host_free(p)
+    return e2e_s
+
+
 def batched_leg(args, torch, flush, with_cpu: bool, with_baseline: bool = True, ngraphs: int | None = None):
     """The batched workload (4,096 graphs in one persistent launch): graphs/s,
     the plain one-graph-per-launch peel beside it, and the CPU bucket peel over
@@ -363,6 +401,9 @@ def main():
                     help="--config 4: the first N graphs of the batch only (a small case for ncu)")
     ap.add_argument("--profile", action="store_true",
                     help="device legs only (no e2e, CPU or reference-GPU legs): the command profiled by ncu")
+    ap.add_argument("--profile-e2e", action="store_true",
+                    help="--config 1-3: the one-shot end-to-end leg alone (upload, device-side CSR check, "
+                         "peel, download): the command profiled by ncu for the CSR check")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -445,6 +486,13 @@ def main():
     if not (np.array_equal(core, want) and kmax == wk):
         raise SystemExit("bench: GPU core numbers differ from the oracle")
 
+    if args.profile_e2e:
+        e2e_ms = e2e_leg(args, kc, V, arcs, off, nbr, want, flush, torch) * 1e3
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "e2e_ms": e2e_ms, "workload": W.SINGLE[args.config]["name"]}),
+                  flush=True)
+        return
+
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.zero_()
@@ -478,39 +526,7 @@ def main():
                               "workload": W.SINGLE[args.config]["name"]}), flush=True)
         return
 
-    # end to end through the public one-shot call: pinned H2D of the CSR, the
-    # peel, D2H of the core numbers, every step
-    lib = kc.lib()
-    h_off = lib.kc_host_alloc(4 * (V + 1))
-    h_nbr = lib.kc_host_alloc(4 * max(arcs, 1))
-    h_core = lib.kc_host_alloc(4 * max(V, 1))
-    a_off = np.ctypeslib.as_array(C.cast(h_off, C.POINTER(C.c_uint32)), shape=(V + 1,))
-    a_nbr = np.ctypeslib.as_array(C.cast(h_nbr, C.POINTER(C.c_uint32)), shape=(max(arcs, 1),))
-    a_off[:] = off
-    a_nbr[:arcs] = nbr
-    u32p = C.POINTER(C.c_uint32)
-    kout = C.c_uint32()
-
-    def e2e_call():
-        rc = lib.kc_peel_csr(C.cast(h_off, u32p), C.cast(h_nbr, u32p), V, C.cast(h_core, u32p), C.byref(kout))
-        if rc:
-            raise SystemExit(f"kc_peel_csr failed: {rc}")
-
-    for _ in range(max(1, args.warmup)):
-        e2e_call()
-    e2e_t = []
-    for _ in range(args.steps):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_call()
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_t) / len(e2e_t)
-    got = np.ctypeslib.as_array(C.cast(h_core, u32p), shape=(V,))
-    if not np.array_equal(got, want):
-        raise SystemExit("bench: e2e core numbers differ from the oracle")
-    for p in (h_off, h_nbr, h_core):
-        lib.kc_host_free(p)
+    e2e_s = e2e_leg(args, kc, V, arcs, off, nbr, want, flush, torch)
 
     if rank != 0:
         return

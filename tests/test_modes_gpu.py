@@ -1,0 +1,56 @@
+"""GPU parity of the one-graph peel under each of its runtime settings.
+
+The settings are read once per process (KC_CLAIM_CAS: claim by CAS or read
+the state first; KC_TAIL_V: the tail hand-off point, 0 = the persistent
+kernel peels every level; KC_LOCAL_BUDGET: the cascade budget, its minimum
+sending most cascades through the task queue), so each case runs in a fresh
+process.  Every case must give the oracle's core numbers and kmax, through
+both the one-shot entry (kc_peel_csr) and a resident graph peeled twice."""
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = Path(__file__).resolve().parents[1]
+
+CHILD = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+sys.path.insert(0, sys.argv[1] + "/tests")
+import kcoregpu_gb300 as kc
+from oracle import kc_oracle as O
+graphs = [
+    kc.build_csr(*kc.gen_rmat(60_000, 500_000, 42))[:2],
+    kc.build_csr(*kc.gen_chung_lu(80_000, 300_000, 2.1, 8_000.0, 43))[:2],
+    kc.build_csr(*kc.gen_er(20_000, 100_000, 41))[:2],
+    kc.build_csr(*kc.gen_rmat(400_000, 3_400_000, 1))[:2],
+]
+for off, nbr in graphs:
+    want, wk = O.bz(off, nbr)
+    core, k = kc.peel_csr(off, nbr)
+    assert np.array_equal(core, want) and k == wk, "peel_csr differs"
+    g = kc.DeviceGraph(off, nbr)
+    for _ in range(2):
+        core, k, _ = g.peel()
+        assert np.array_equal(core, want) and k == wk, "resident peel differs"
+    g.free()
+print("ok")
+"""
+
+
+@pytest.mark.parametrize("env", [
+    {"KC_CLAIM_CAS": "0"},
+    {"KC_TAIL_V": "0"},
+    {"KC_TAIL_V": "16384"},
+    {"KC_LOCAL_BUDGET": "32"},
+    {"KC_CLAIM_CAS": "0", "KC_TAIL_V": "0", "KC_LOCAL_BUDGET": "32"},
+], ids=lambda e: ",".join(f"{k}={v}" for k, v in e.items()))
+def test_peel_under_each_setting(gpu, env):
+    r = subprocess.run([sys.executable, "-c", CHILD, str(ROOT)], env={**os.environ, **env},
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stderr[-2000:] or r.stdout[-2000:]

@@ -21,16 +21,19 @@ from kcoregpu_gb300 import _lib
 pytestmark = pytest.mark.gpu
 
 
-def _noalloc_peel(torch, off, nbr):
+def _noalloc_peel(torch, off, nbr, shift: int = 0):
+    """shift > 0 places the CSR that many 4-byte words into its device buffers
+    (pointers the caller owns need only 4-byte alignment)."""
     lib = kc.lib()
     V = len(off) - 1
-    d_off = torch.from_numpy(off.view(np.int32)).cuda()
-    d_nbr = torch.from_numpy(nbr.view(np.int32)).cuda()
+    pad = np.zeros(shift, np.int32)
+    d_off = torch.from_numpy(np.concatenate([pad, off.view(np.int32)])).cuda()
+    d_nbr = torch.from_numpy(np.concatenate([pad, nbr.view(np.int32)])).cuda()
     d_core = torch.full((max(V, 1),), -1, dtype=torch.int32, device="cuda")
     kmax = C.c_uint32(12345)
     stream = torch.cuda.current_stream().cuda_stream
-    rc = lib.kc_peel_noalloc(C.c_void_p(d_off.data_ptr()), C.c_void_p(d_nbr.data_ptr()), V, len(nbr),
-                             C.c_void_p(d_core.data_ptr()), C.byref(kmax), C.c_void_p(stream))
+    rc = lib.kc_peel_noalloc(C.c_void_p(d_off.data_ptr() + 4 * shift), C.c_void_p(d_nbr.data_ptr() + 4 * shift), V,
+                             len(nbr), C.c_void_p(d_core.data_ptr()), C.byref(kmax), C.c_void_p(stream))
     _lib.check(rc, "kc_peel_noalloc")
     return d_core[:V].cpu().numpy().view(np.uint32), kmax.value
 
@@ -75,3 +78,21 @@ def test_noalloc_refuses_an_invalid_csr_before_peeling(gpu):
     got, gk = _noalloc_peel(torch, off, nbr)
     np.testing.assert_array_equal(got, want)
     assert gk == wk
+
+
+def test_noalloc_accepts_csr_arrays_at_4_byte_alignment(gpu):
+    # Offsets and neighbour ids that start one word into their buffers: the
+    # device-side CSR check then reads them with 4-byte loads instead of
+    # 16-byte ones, and both the check and the peel give the same results.
+    torch = pytest.importorskip("torch")
+    off, nbr = kc.build_csr(*kc.gen_rmat(200_000, 1_500_000, seed=24))[:2]
+    want, wk = kc.peel_csr(off, nbr)
+    for shift in (1, 2, 3):
+        got, gk = _noalloc_peel(torch, off, nbr, shift)
+        np.testing.assert_array_equal(got, want)
+        assert gk == wk
+    bad = nbr.copy()
+    bad[-5] = len(off) - 1
+    with pytest.raises(kc.KCoreError) as e:
+        _noalloc_peel(torch, off, bad, 1)
+    assert e.value.name == "KC_ERR_INVALID"
