@@ -9,11 +9,12 @@
 //
 // GB300 design (no reference counterpart):
 //  * w[v] holds deg(v) + kBias.  Bit 31 (kClaim) marks a vertex as peeled
-//    ("claimed").  A vertex is claimed exactly once, by an atomicOr that sees
-//    the bit clear, either by the frontier scan (w == level+kBias) or by the
-//    walker whose decrement took w from level+1 to level (ours.cc:96; when
-//    the walker read level+1 before, one atomicCAS decrements and claims).
-//    The bias keeps transient over-decrements (stale readers that are undone,
+//    ("claimed").  A vertex is claimed exactly once, by one atomic that sees
+//    the bit clear: the frontier scan's atomicOr (w == level+kBias), a
+//    walker's atomicCAS(level+1 -> level | claim), which decrements and
+//    claims at once, or the atomicOr of the walker whose atomicSub took w
+//    from level+1 to level (ours.cc:96).  The bias keeps transient
+//    over-decrements (decrements that raced below the level and are undone,
 //    as in ours.cc:102-105) from ever borrowing into the claim bit.
 //  * Because claims are exclusive, the scan and the neighbour walk of one
 //    level run concurrently: scan hits are walked inline by the scanning warp,
