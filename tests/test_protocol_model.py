@@ -66,7 +66,7 @@ def run(parts: int, seed: int, max_children: int = 3, max_tasks: int = 200, fini
                 # a planted mistake: the task publishes its finish before its
                 # last push, so a snapshot between the two shows the level done
                 units, tail = word >> HALF, word & MASK
-                assert (units == parts + tail) == (not scanning and queued == 0 and not running)
+                assert units != parts + tail, "the level reads complete while a push is pending"
                 word += 1
                 queued += 1
                 pushed_total += 1
@@ -76,11 +76,11 @@ def run(parts: int, seed: int, max_children: int = 3, max_tasks: int = 200, fini
 def test_completion_word_is_exact_under_random_interleavings(parts):
     pushed = 0
     for seed in range(25):
-        pushed += run(parts, seed)
+        pushed += run(parts, seed, max_children=seed % 4)   # shallow to capped task trees
     assert pushed > 0
 
 
 def test_the_model_catches_a_finish_published_before_a_push():
     with pytest.raises(AssertionError):
         for seed in range(25):
-            run(2, seed, finish_first=True)
+            run(2, seed, max_children=0, finish_first=True)
