@@ -195,6 +195,16 @@ __device__ __forceinline__ void decrement4(const PeelArgs& a, const uint32_t (&u
     }
 }
 
+// Starts moving the first adjacency line(s) of a vertex just claimed, arcs
+// [start, start+len), into L1: the walk step that reads them comes one claim
+// later, and the adjacency is read-only while the peel runs.  Hubs go to the
+// task queue, where another SM reads them, and get none.
+__device__ __forceinline__ void prefetch_adjacency(const PeelArgs& a, uint32_t start, uint32_t len) {
+    if (len == 0 || len > kLocalArcs) return;
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(a.nbr + start));
+    if ((start & 31u) + len > 32u) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.nbr + ((start | 31u) + 1u)));
+}
+
 // Plain decrements issued by a walk step whose results have not been
 // examined yet (u = kFull: none).
 struct PendingDec {
@@ -268,6 +278,7 @@ __device__ __forceinline__ void claim_or_defer(Warp& w, const uint32_t (&u)[4], 
         if (u[j] == kFull) continue;
         if (old[j] == kk + 1) {
             f[j] = true; start[j] = s0[j]; len[j] = s1[j] - s0[j];
+            prefetch_adjacency(a, start[j], len[j]);
         } else if (old[j] > kk + 1 && old[j] < kClaim) {
             pd.u[j] = u[j];
             pd.old[j] = atomicSub(a.w + u[j], 1u);
@@ -446,7 +457,11 @@ __device__ __forceinline__ unsigned claim_hits(Warp& w, const uint32_t (&v)[4], 
     unsigned mine = 0;
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-        if (!(o[j] & kClaim)) { mine |= 1u << j; w.a.core[v[j]] = w.level; }
+        if (!(o[j] & kClaim)) {
+            mine |= 1u << j;
+            w.a.core[v[j]] = w.level;
+            if (w.level > 0) prefetch_adjacency(w.a, s0[j], s1[j] - s0[j]);
+        }
     return mine;
 }
 
