@@ -148,6 +148,16 @@ __device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u, uint
     if (__ballot_sync(kFull, glob)) push_tasks(w, glob, start, len);
 }
 
+// Starts moving the first adjacency line(s) of a vertex just claimed, arcs
+// [start, start+len), into L1: the walk step that reads them comes one claim
+// later, and the adjacency is read-only while the peel runs.  Hubs go to the
+// task queue, where another SM reads them, and get none.
+__device__ __forceinline__ void prefetch_adjacency(const PeelArgs& a, uint32_t start, uint32_t len) {
+    if (len == 0 || len > kLocalArcs) return;
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(a.nbr + start));
+    if ((start & 31u) + len > 32u) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.nbr + ((start | 31u) + 1u)));
+}
+
 // The neighbours u[j] of vertices peeled at this level (ours.cc:91-106), d[j]
 // their states as read before: f[j] is set when this thread's decrement took
 // u[j] to the level and claimed it, with u[j]'s arc range in start[j] / len[j].
@@ -179,7 +189,11 @@ __device__ __forceinline__ void decrement4(const PeelArgs& a, const uint32_t (&u
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         if (cas & (1u << j)) {
-            if (old[j] == kk + 1) { f[j] = true; start[j] = s0[j]; len[j] = s1[j] - s0[j]; continue; }
+            if (old[j] == kk + 1) {
+                f[j] = true; start[j] = s0[j]; len[j] = s1[j] - s0[j];
+                prefetch_adjacency(a, start[j], len[j]);
+                continue;
+            }
             if (!(old[j] > kk && old[j] < kClaim)) continue;
             old[j] = atomicSub(a.w + u[j], 1u);   // lost race: the plain rule with the value seen
         } else if (!(sub & (1u << j))) {
@@ -189,20 +203,11 @@ __device__ __forceinline__ void decrement4(const PeelArgs& a, const uint32_t (&u
             const uint32_t t0 = KC_LDG(a.off + u[j]), t1 = KC_LDG(a.off + u[j] + 1);
             if (atomicOr(a.w + u[j], kClaim) & kClaim) continue;
             f[j] = true; start[j] = t0; len[j] = t1 - t0;
+            prefetch_adjacency(a, start[j], len[j]);
         } else if (old[j] <= kk || old[j] >= kClaim) {
             atomicAdd(a.w + u[j], 1u);   // undo
         }
     }
-}
-
-// Starts moving the first adjacency line(s) of a vertex just claimed, arcs
-// [start, start+len), into L1: the walk step that reads them comes one claim
-// later, and the adjacency is read-only while the peel runs.  Hubs go to the
-// task queue, where another SM reads them, and get none.
-__device__ __forceinline__ void prefetch_adjacency(const PeelArgs& a, uint32_t start, uint32_t len) {
-    if (len == 0 || len > kLocalArcs) return;
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(a.nbr + start));
-    if ((start & 31u) + len > 32u) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.nbr + ((start | 31u) + 1u)));
 }
 
 // Plain decrements issued by a walk step whose results have not been
