@@ -239,7 +239,9 @@ int kc_batch_upload(const kc_segcsr* s, kc_batch** out) {
     b->bits_cap = std::min(vmax, kBatchBitsMax);
     b->bits_bytes = (size_t)((b->bits_cap + 31) / 32) * 4;
     // static plus dynamic shared memory may exceed the default 48 KB window
-    cudaFuncSetAttribute(peel_batch_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->bits_bytes);
+    if (cudaError_t ea = cudaFuncSetAttribute(peel_batch_fn(), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)b->bits_bytes))
+        return fail(cuda_fail(ea, "cudaFuncSetAttribute(peel_batch_kernel)"));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_batch_fn(), kBatchThreads, b->bits_bytes);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gper, peel_persistent_fn(), kPeelThreads, 0);
     b->ggrid = gper > 0 ? sms : 0;   // giants: one CTA per SM, as the single-graph peel

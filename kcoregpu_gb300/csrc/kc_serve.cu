@@ -746,7 +746,12 @@ int kc_serve_open(const kc_serve_cfg* cfg, kc_server** out) {
     s->bits_cap = std::min(s->cfg.small_vertices, kBatchBitsMax);
     s->bits_bytes = (size_t)((s->bits_cap + 31) / 32) * 4;
     // static plus dynamic shared memory exceeds the default 48 KB window
-    cudaFuncSetAttribute((const void*)serve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->bits_bytes);
+    if (cudaError_t ea = cudaFuncSetAttribute((const void*)serve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)s->bits_bytes)) {
+        const int rc = cuda_fail(ea, "cudaFuncSetAttribute(serve_kernel)");
+        delete s;
+        return rc;
+    }
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, (const void*)serve_kernel, kPeelThreads, s->bits_bytes);
     s->grid = sms * std::max(1, per);
     if (!s->cfg.max_gang || s->cfg.max_gang > (uint32_t)s->grid) s->cfg.max_gang = (uint32_t)s->grid;
