@@ -1,17 +1,23 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 k-core peel (one JSON line on rank 0).
 
-Default workload: the single-graph R-MAT scale-20 edge-factor-5 peel (1,048,576
-vertices, 5,242,880 directed draws, a/b/c/d = .57/.19/.19/.05, seed 2),
-symmetrised and deduplicated, uint32 CSR resident in HBM.  A step is one full
-peel of that graph (every level until all vertices are peeled).
+Headline workload (default): the single-graph peel of the skewed Chung-Lu
+graph (2,400,000 vertices, 5,000,000 undirected edges, degree exponent 2.1,
+max expected degree 100,000, seed 3), uint32 CSR resident in HBM.  A step is
+one full peel of that graph (every level until all vertices are peeled).  The
+same line carries, as sub-records with their own roofline, the two R-MAT
+single-graph workloads (400K vertices / 3.4M draws, and scale 20 edge factor
+5), the batched workload (4,096 graphs in one persistent launch) and the
+served workload (a Poisson stream of 120 requests plus the R-MAT scale-24
+edge-factor-16 graph, every result checked against the CPU oracle).
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|2|3] [--impl ours|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--config 1|2|3|4|5] [--impl ours|reference]
 
 --impl reference times the reference algorithm's CPU restatement (the
 level-synchronous peel of src/ours.cc:117-160, oracle/kc_oracle.c) on all host
-cores; the reference has no CPU peel of its own.  Multi-GPU runs are replicas
-(one independent graph per rank, no collective on the data path).
+cores, on input graphs built by the oracle's own generators: that arm loads no
+library of the product.  Multi-GPU runs are replicas (one independent graph per
+rank, no collective on the data path).
 """
 from __future__ import annotations
 
@@ -33,12 +39,14 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "k-core edges/s & HBM GB/s; batched graphs/s, p50/p99 latency vs plain peel"
 L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
+TIMING_NOTE = ("GPU arm: L2 flushed between timed steps (512 MiB write), inputs resident in HBM; "
+               "reference arm: host memory")
 
 # DRAM bytes (read + write) of one peel -- the persistent kernel plus the
-# one-CTA tail kernel it hands the last levels to -- from one ncu capture of
-# the same workload (profiles/peel_persistent_rmat-s20-ef5.md); None where not
-# captured.
-NCU_TRAFFIC = {2: 45_338_880 + 3_630_080 + 7_795_712 + 0}
+# one-CTA tail kernel it hands the last levels to -- per workload, from one ncu
+# capture of that workload with the build that is measured here; None where
+# not captured.
+NCU_TRAFFIC = {1: None, 2: 45_338_880 + 3_630_080 + 7_795_712, 3: None}
 
 
 def dist_env():
@@ -117,20 +125,42 @@ def cpu_model() -> str:
     return platform.processor() or platform.machine()
 
 
+def single_config(cfg: int, V: int, arcs: int, kmax: int) -> dict:
+    """The `config` of a single-graph line; both arms print the same one."""
+    from kcoregpu_gb300 import workloads as W
+    return {"workload": W.SINGLE[cfg]["name"], "V": V, "undirected_edges": arcs // 2, "arcs": arcs,
+            "kmax": kmax, "levels": kmax + 1, "timing": TIMING_NOTE}
+
+
+def graphs_config(cfg: int) -> dict:
+    """The `config` of a batched or served line; both arms print the same one."""
+    from kcoregpu_gb300 import workloads as W
+    if cfg == 4:
+        return {"workload": W.BATCH["name"], "graphs": W.BATCH["ngraphs"], "timing": TIMING_NOTE}
+    return {"workload": W.SERVED["name"], "requests": SERVED_REQUESTS + 1, "timing": TIMING_NOTE}
+
+
+SERVED_REQUESTS = 120
+SERVED_RATES = [25, 50, 100, 200, 400, 800]
+
+
 def reference_arm(args, rank, world):
-    """The reference algorithm on the host cores (CPU restatement, all threads)."""
+    """The reference algorithm on the host cores (CPU restatement, all
+    threads), on inputs from the oracle's generators."""
     if rank != 0:
         return
     if args.config in (4, 5):
         return reference_arm_graphs(args, world)
-    from kcoregpu_gb300 import workloads as W
     from oracle import kc_oracle as O
-    off, nbr = W.single_graph(args.config)
-    m = len(nbr) // 2
+    from oracle import kc_workloads as OW
+    off, nbr = OW.single_graph(args.config)
+    V, arcs = len(off) - 1, len(nbr)
+    m = arcs // 2
     nth = os.cpu_count() or 1
     for _ in range(args.warmup):
         O.levelsync(off, nbr, nthreads=nth)
     times = []
+    kmax = levels = 0
     for _ in range(args.steps):
         t0 = time.perf_counter()
         _, kmax, levels = O.levelsync(off, nbr, nthreads=nth)
@@ -141,8 +171,7 @@ def reference_arm(args, rank, world):
         "impl": "reference", "metric": METRIC, "value": val, "unit": "edges/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": W.SINGLE[args.config]["name"], "V": len(off) - 1, "undirected_edges": m,
-                   "kmax": kmax, "levels": levels},
+        "config": single_config(args.config, V, arcs, kmax),
         "cpu_baseline": {"value": val, "unit": "edges/s", "cores": nth, "kind": "port",
                          "sample": f"full graph x {args.steps} peels (level-synchronous restatement of "
                                    f"src/ours.cc:117-160, OpenMP, {cpu_model()})"},
@@ -155,16 +184,16 @@ def reference_arm_graphs(args, world, sample: int = 48):
     restatement (all threads) over a bounded sample of the workload's graphs
     (the first `sample` graphs of the batch, or requests of the stream),
     reported as graphs/s."""
-    from kcoregpu_gb300 import workloads as W
     from oracle import kc_oracle as O
+    from oracle import kc_workloads as OW
     nth = os.cpu_count() or 1
     if args.config == 4:
-        seg = W.batch(sample)
+        seg = OW.batch(sample)
         graphs = [seg.graph(g) for g in range(seg.ngraphs)]
-        name, what = W.BATCH["name"], f"graphs 0..{sample - 1} of the batch"
+        what = f"graphs 0..{sample - 1} of the batch"
     else:
-        graphs = [W.served_request(i) for i in range(sample)]
-        name, what = W.SERVED["name"], f"requests 0..{sample - 1} of the stream (no scale-24 graph)"
+        graphs = [OW.served_request(i) for i in range(sample)]
+        what = f"requests 0..{sample - 1} of the stream (no scale-24 graph)"
     for off, nbr in graphs[: max(1, args.warmup)]:
         O.levelsync(off, nbr, nthreads=nth)
     times = []
@@ -179,7 +208,7 @@ def reference_arm_graphs(args, world, sample: int = 48):
         "impl": "reference", "metric": METRIC, "value": val, "unit": "graphs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": name, "sample_graphs": len(graphs)},
+        "config": graphs_config(args.config),
         "cpu_baseline": {"value": val, "unit": "graphs/s", "cores": nth, "kind": "port",
                          "sample": f"{what}, level-synchronous restatement of src/ours.cc:117-160, "
                                    f"OpenMP, {cpu_model()}"},
@@ -275,6 +304,89 @@ def e2e_leg(args, kc, V: int, arcs: int, off, nbr, want, flush, torch) -> float:
     return e2e_s
 
 
+def single_leg(cfg: int, args, torch, flush, local: int, world: int, steps: int, warmup: int,
+               full: bool = True) -> dict:
+    """One single-graph workload: the device-timed peel (value), its roofline,
+    and -- with `full` -- the e2e call, the CPU BZ and the reference's own
+    GPU kernels beside it."""
+    import kcoregpu_gb300 as kc
+    from kcoregpu_gb300 import workloads as W
+    from oracle import kc_oracle as O
+    off, nbr = W.single_graph(cfg)
+    V, arcs = len(off) - 1, len(nbr)
+    m = arcs // 2
+    stream = torch.cuda.Stream()
+    g = kc.DeviceGraph(off, nbr)
+    g.set_stream(stream.cuda_stream)
+
+    # correctness of the benchmarked graph (untimed)
+    core, kmax, _ = g.peel()
+    want, wk = O.bz(off, nbr)
+    if not (np.array_equal(core, want) and kmax == wk):
+        raise SystemExit(f"bench: GPU core numbers differ from the oracle on {W.SINGLE[cfg]['name']}")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            flush.zero_()
+            g.peel_async()
+        stream.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        kern_ms = []
+        barrier()
+        torch.cuda.synchronize()
+        with Clocks(local) as clk:
+            t_wall = time.perf_counter()
+            for i in range(steps):
+                flush.zero_()                   # L2 flushed between timed steps
+                starts[i].record(stream)
+                g.peel_async()
+                ends[i].record(stream)
+                _, _, st = g.fetch(want_core=False)   # kernel-only time from the library's events
+                kern_ms.append(st["peel_ms"])
+            torch.cuda.synchronize()
+            t_wall = time.perf_counter() - t_wall
+        barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = sum(step_ms) / len(step_ms)
+    kms = sum(kern_ms) / len(kern_ms)
+    ms, kms = max_over_ranks([ms, kms], world, device="cuda")
+    peak, peak_kind = measured_peak_hbm()
+    B = W.algorithmic_bytes(V, arcs, kmax)
+    achieved = B / (kms / 1e3) / 1e9
+    rec = {"workload": W.SINGLE[cfg]["name"], "config": single_config(cfg, V, arcs, kmax),
+           "steps": steps, "warmup": warmup, "ms_per_step": ms, "kernel_ms": kms,
+           "edges_per_s": world * m / (ms / 1e3), "arcs_per_s": world * arcs / (ms / 1e3),
+           "hbm_gbs": achieved,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak, "peak_kind": peak_kind + " hbm_gbs",
+                        "algorithmic_bytes": B, "traffic": NCU_TRAFFIC.get(cfg)},
+           "gpu_launches": 2 * steps,   # persistent peel + tail kernel per step
+           "clocks": clk.summary(), "wall_s": t_wall, "bit_exact_vs_oracle": True}
+    if args.profile:
+        g.free()
+        return rec
+    if full:
+        e2e_s = e2e_leg(argparse.Namespace(steps=steps, warmup=warmup), kc, V, arcs, off, nbr, want, flush, torch)
+        rec["e2e"] = {"value": world * m / e2e_s, "unit": "edges/s", "ms": e2e_s * 1e3,
+                      "h2d_bytes_per_step": 4 * (V + 1) + 4 * arcs, "d2h_bytes_per_step": 4 * V}
+        if not args.no_cpu:
+            rec["cpu_baseline"] = cpu_baseline(off, nbr)
+        import tempfile
+        with tempfile.TemporaryDirectory() as td:
+            ref = reference_gpu(off, nbr, Path(td))
+            if ref is not None and "core" in ref:
+                ref["bit_exact_vs_oracle"] = bool(np.array_equal(ref.pop("core"), want))
+        if ref is not None:
+            rec["reference_gpu"] = ref
+    g.free()
+    return rec
+
+
 def batched_leg(args, torch, flush, with_cpu: bool, with_baseline: bool = True, ngraphs: int | None = None):
     """The batched workload (4,096 graphs in one persistent launch): graphs/s,
     the plain one-graph-per-launch peel beside it, and the CPU bucket peel over
@@ -310,28 +422,38 @@ def batched_leg(args, torch, flush, with_cpu: bool, with_baseline: bool = True, 
     B_alg = W.batch_algorithmic_bytes(seg, kmax)
     peak, _ = measured_peak_hbm()
     out = {"workload": W.BATCH["name"], "graphs": G, "V": Vt, "arcs": At, "generation_s": gen_s,
-           "graphs_per_s": G / (step_ms / 1e3), "ms_per_step": step_ms,
+           "graphs_per_s": G / (step_ms / 1e3), "ms_per_step": step_ms, "steps": args.steps,
            "edges_per_s": (At // 2) / (step_ms / 1e3), "hbm_gbs": B_alg / (step_ms / 1e3) / 1e9,
            "roofline_frac": B_alg / (step_ms / 1e3) / 1e9 / peak, "algorithmic_bytes": B_alg,
            "plan": {k: v for k, v in b.plan().items() if k != "schedule"},
-           "kmax_max": int(kmax.max())}
+           "kmax_max": int(kmax.max()), "bit_exact_vs_oracle": True}
     if per_graph_ms is not None:
         out["plain_per_graph"] = {"ms": per_graph_ms, "graphs_per_s": G / (per_graph_ms / 1e3),
                                   "speedup_of_batched": per_graph_ms / step_ms}
     if with_cpu:
         out["cpu_baseline"] = {"value": G / cpu_s, "unit": "graphs/s", "cores": O.num_threads(),
-                               "kind": "port", "sample": "all 4,096 graphs, one Batagelj-Zaversnik per graph, "
+                               "kind": "port", "sample": f"all {G:,} graphs, one Batagelj-Zaversnik per graph, "
                                                          "OpenMP over graphs"}
     b.free()
     return out
 
 
-def served_leg(requests: int, mmax: int | None, with_big: bool, rates, seed: int = 5):
+def _oracle_all(graphs):
+    """BZ core numbers and kmax of every graph, on all host cores (the calls
+    release the GIL)."""
+    import concurrent.futures as cf
+    from oracle import kc_oracle as O
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        return list(ex.map(lambda g: O.bz(*g), graphs))
+
+
+def served_leg(requests: int, mmax: int | None, with_big: bool, rates, seed: int = 5, saturated_passes: int = 3):
     """Continuous batching: a seeded Poisson stream of requests submitted to the
-    server at each arrival rate (and all at once for saturation); latency is
-    submit -> core numbers on the host.  The plain one-graph-at-a-time peel
-    (kc_peel_csr per request, upload and download included) runs the same
-    stream for comparison."""
+    server at each arrival rate, then all at once (saturation) in
+    `saturated_passes` back-to-back passes; latency is submit -> core numbers
+    on the host.  Every result of every pass is compared with the CPU BZ peel.
+    The plain one-graph-at-a-time peel (kc_peel_csr per request, upload and
+    download included) runs the same stream for comparison."""
     import kcoregpu_gb300 as kc
     from kcoregpu_gb300 import workloads as W
     from kcoregpu_gb300.serve import Server
@@ -342,14 +464,27 @@ def served_leg(requests: int, mmax: int | None, with_big: bool, rates, seed: int
         big_pos = requests // 2
         reqs.insert(big_pos, W.served_big())
     gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    wants = _oracle_all(reqs)
+    oracle_s = time.perf_counter() - t0
     edges = [len(n) // 2 for _, n in reqs]
+    mismatches = 0
+    checked = 0
+
+    def check(res):
+        nonlocal mismatches, checked
+        for (core, kmax, _), (wc, wk) in zip(res, wants):
+            checked += 1
+            if kmax != wk or not np.array_equal(core, wc):
+                mismatches += 1
+
     srv = Server()
     srv.wait(srv.submit(*reqs[0]))   # warm-up (kernel launch, pool growth)
     if big_pos is not None:          # and the big graph's own pool growth and first device touch
         srv.wait(srv.submit(*reqs[big_pos]))
     rng = np.random.default_rng(seed)
     sweep = []
-    for rate in list(rates) + [None]:
+    for rate in list(rates) + [None] * saturated_passes:
         gaps = rng.exponential(1.0 / rate, len(reqs)) if rate else np.zeros(len(reqs))
         arrive = np.cumsum(gaps) - gaps[0]
         ids = []
@@ -360,13 +495,16 @@ def served_leg(requests: int, mmax: int | None, with_big: bool, rates, seed: int
             ids.append(srv.submit(o, n))
         res = [srv.wait(r, timeout_s=300) for r in ids]
         span = time.perf_counter() - start
+        check(res)
         lat = np.array([t["latency_us"] for _, _, t in res]) / 1e3
         pt = {"rate": rate or "all-at-once", "graphs_per_s": len(reqs) / span, "edges_per_s": sum(edges) / span,
               "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
               "max_gang": max(t["gang"] for _, _, t in res)}
         if big_pos is not None:
             pt["big_graph_latency_ms"] = float(lat[big_pos])
+            pt["big_graph_peel_ms"] = res[big_pos][2]["peel_us"] / 1e3
         sweep.append(pt)
+        del res
     st = srv.stats()
     srv.close()
     # the same warm-up as the server's: the first call and the big graph's
@@ -375,16 +513,25 @@ def served_leg(requests: int, mmax: int | None, with_big: bool, rates, seed: int
     if big_pos is not None:
         kc.peel_csr(*reqs[big_pos])
     t1 = time.perf_counter()
-    for o, n in reqs:
-        kc.peel_csr(o, n)
+    plain = [kc.peel_csr(o, n) for o, n in reqs]
     plain_s = time.perf_counter() - t1
-    sat = sweep[-1]
+    plain_bad = sum(1 for (c, k), (wc, wk) in zip(plain, wants) if k != wk or not np.array_equal(c, wc))
+    sat = sweep[-saturated_passes:]
+    gps = [p["graphs_per_s"] for p in sat]
+    p50 = [p["p50_ms"] for p in sat]
+    p99 = [p["p99_ms"] for p in sat]
     return {"workload": W.SERVED["name"] if with_big else f"served-{requests}-requests-m<= {mmax}",
             "requests": len(reqs), "undirected_edges": int(sum(edges)), "generation_s": gen_s,
-            "sweep": sweep, "saturated_graphs_per_s": sat["graphs_per_s"],
+            "oracle_s": oracle_s, "sweep": sweep,
+            "saturated_graphs_per_s": statistics.median(gps),
+            "saturated_passes": {"graphs_per_s": gps, "p50_ms": p50, "p99_ms": p99,
+                                 "p50_spread": max(p50) / min(p50) if min(p50) > 0 else None,
+                                 "p99_spread": max(p99) / min(p99) if min(p99) > 0 else None},
+            "bit_exact": mismatches == 0 and plain_bad == 0, "results_checked": checked + len(plain),
+            "mismatches": mismatches + plain_bad,
             "plain_one_at_a_time": {"graphs_per_s": len(reqs) / plain_s, "seconds": plain_s,
-                                    "speedup_of_served": sat["graphs_per_s"] / (len(reqs) / plain_s)},
-            "peak_device_bytes": st["peak_in_use"], "blocks": st["blocks"]}
+                                    "speedup_of_served": statistics.median(gps) / (len(reqs) / plain_s)},
+            "peak_device_bytes": st["peak_in_use"], "blocks": st["blocks"], "direct": st["direct"]}
 
 
 def main():
@@ -392,11 +539,12 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
-    ap.add_argument("--no-serve", action="store_true", help="skip the served leg of the default run")
+    ap.add_argument("--config", type=int, default=3, choices=[1, 2, 3, 4, 5])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="skip the other single-graph workloads' sub-records")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched leg of the default run")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served leg of the default run")
     ap.add_argument("--graphs", type=int, default=None,
                     help="--config 4: the first N graphs of the batch only (a small case for ncu)")
     ap.add_argument("--profile", action="store_true",
@@ -426,17 +574,17 @@ def main():
     if args.config == 5:
         barrier()
         with Clocks(local) as clk:
-            sv = served_leg(W_requests := 120, None, True, rates=[25, 50, 100, 200, 400, 800])
+            sv = served_leg(SERVED_REQUESTS, None, True, rates=SERVED_RATES)
         barrier()
         if rank == 0:
-            sat = sv["sweep"][-1]
+            sat = sv["saturated_passes"]
             line = {"metric": METRIC, "value": world * sv["saturated_graphs_per_s"], "unit": "graphs/s",
-                    "n_gpus": world, "steps": W_requests, "warmup": 1, "ms_per_step": 1e3 / sv["saturated_graphs_per_s"],
+                    "n_gpus": world, "steps": sv["requests"], "warmup": 1,
+                    "ms_per_step": 1e3 / sv["saturated_graphs_per_s"],
                     "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-                    "data": "synthetic", "config": {"workload": sv["workload"], "requests": sv["requests"],
-                                                    "undirected_edges": sv["undirected_edges"],
-                                                    "inputs": "host memory, uploaded per request"},
-                    "p50_ms": sat["p50_ms"], "p99_ms": sat["p99_ms"],
+                    "data": "synthetic", "config": graphs_config(5),
+                    "p50_ms": statistics.median(sat["p50_ms"]), "p99_ms": statistics.median(sat["p99_ms"]),
+                    "bit_exact": sv["bit_exact"],
                     "e2e": {"value": world * sv["saturated_graphs_per_s"], "unit": "graphs/s",
                             "note": "every request's upload and result download are inside its latency"},
                     "clocks": clk.summary(), "served": sv}
@@ -459,10 +607,7 @@ def main():
             line = {"metric": METRIC, "value": world * bl["graphs_per_s"], "unit": "graphs/s", "n_gpus": world,
                     "steps": args.steps, "warmup": args.warmup, "ms_per_step": bl["ms_per_step"],
                     "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-                    "data": "synthetic", "config": {"workload": bl["workload"], "graphs": bl["graphs"],
-                                                    "V": bl["V"], "arcs": bl["arcs"],
-                                                    "l2": "flushed between timed steps (512 MiB write)",
-                                                    "inputs": "resident in HBM"},
+                    "data": "synthetic", "config": graphs_config(4),
                     "roofline": {"bound": "hbm", "achieved": bl["hbm_gbs"], "peak": measured_peak_hbm()[0],
                                  "unit": "GB/s", "frac": bl["roofline_frac"], "traffic": None,
                                  "algorithmic_bytes": bl["algorithmic_bytes"]},
@@ -472,107 +617,62 @@ def main():
             print(json.dumps(line), flush=True)
         return
 
-    off, nbr = W.single_graph(args.config)
-    V, arcs = len(off) - 1, len(nbr)
-    m = arcs // 2
-    stream = torch.cuda.Stream()
-    g = kc.DeviceGraph(off, nbr)
-    g.set_stream(stream.cuda_stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
-
-    # correctness of the benchmarked graph (untimed)
-    core, kmax, st0 = g.peel()
-    want, wk = O.bz(off, nbr)
-    if not (np.array_equal(core, want) and kmax == wk):
-        raise SystemExit("bench: GPU core numbers differ from the oracle")
-
     if args.profile_e2e:
-        e2e_ms = e2e_leg(args, kc, V, arcs, off, nbr, want, flush, torch) * 1e3
+        off, nbr = W.single_graph(args.config)
+        want, _ = O.bz(off, nbr)
+        e2e_ms = e2e_leg(args, kc, len(off) - 1, len(nbr), off, nbr, want, flush, torch) * 1e3
         if rank == 0:
             print(json.dumps({"profile_run": True, "e2e_ms": e2e_ms, "workload": W.SINGLE[args.config]["name"]}),
                   flush=True)
         return
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            flush.zero_()
-            g.peel_async()
-        stream.synchronize()
-        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-        kern_ms = []
-        barrier()
-        torch.cuda.synchronize()
-        with Clocks(local) as clk:
-            t_wall = time.perf_counter()
-            for i in range(args.steps):
-                flush.zero_()                   # L2 flushed between timed steps
-                starts[i].record(stream)
-                g.peel_async()
-                ends[i].record(stream)
-                _, _, st = g.fetch(want_core=False)   # kernel-only time from the library's events
-                kern_ms.append(st["peel_ms"])
-            torch.cuda.synchronize()
-            t_wall = time.perf_counter() - t_wall
-        barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = sum(step_ms) / len(step_ms)
-    kms = sum(kern_ms) / len(kern_ms)
-    ms, kms = max_over_ranks([ms, kms], world, device="cuda")
-
+    head = single_leg(args.config, args, torch, flush, local, world, args.steps, args.warmup, full=True)
     if args.profile:
         if rank == 0:
-            print(json.dumps({"profile_run": True, "ms_per_step": ms, "kernel_ms": kms,
-                              "workload": W.SINGLE[args.config]["name"]}), flush=True)
+            print(json.dumps({"profile_run": True, "ms_per_step": head["ms_per_step"],
+                              "kernel_ms": head["kernel_ms"], "workload": head["workload"]}), flush=True)
         return
-
-    e2e_s = e2e_leg(args, kc, V, arcs, off, nbr, want, flush, torch)
-
-    if rank != 0:
+    if rank != 0 and world > 1:
         return
-    peak, peak_kind = measured_peak_hbm()
-    B = W.algorithmic_bytes(V, arcs, kmax)
-    achieved = B / (kms / 1e3) / 1e9
-    value = world * m / (ms / 1e3)
     line = {
-        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": head["edges_per_s"], "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": W.SINGLE[args.config]["name"], "V": V, "undirected_edges": m, "arcs": arcs,
-                   "kmax": kmax, "levels": kmax + 1, "parallelism": f"replicas{world}",
-                   "l2": "flushed between timed steps (512 MiB write)", "inputs": "resident in HBM"},
-        "hbm_gbs": achieved, "arcs_per_s": world * arcs / (ms / 1e3),
-        "kernel_ms": kms,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind + " hbm_gbs",
-                     "algorithmic_bytes": B,
-                     "traffic": NCU_TRAFFIC.get(args.config)},
-        "e2e": {"value": world * m / e2e_s, "unit": "edges/s", "ms": e2e_s * 1e3,
-                "h2d_bytes_per_step": 4 * (V + 1) + 4 * arcs, "d2h_bytes_per_step": 4 * V},
-        "gpu_launches": 2 * args.steps,   # persistent peel + tail kernel per step
-        "clocks": clk.summary(),
-        "wall_s": t_wall,
+        "config": head["config"], "parallelism": f"replicas{world}",
+        "hbm_gbs": head["hbm_gbs"], "arcs_per_s": head["arcs_per_s"], "kernel_ms": head["kernel_ms"],
+        "roofline": head["roofline"], "e2e": head["e2e"], "gpu_launches": head["gpu_launches"],
+        "clocks": head["clocks"], "wall_s": head["wall_s"], "bit_exact_vs_oracle": True,
     }
-    if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(off, nbr)
-    import tempfile
-    with tempfile.TemporaryDirectory() as td:
-        ref = reference_gpu(off, nbr, Path(td))
-        if ref is not None and "core" in ref:
-            ref["bit_exact_vs_oracle"] = bool(np.array_equal(ref.pop("core"), want))
-    if ref is not None:
-        line["reference_gpu"] = ref
-    if not args.no_batch:
+    for k in ("cpu_baseline", "reference_gpu"):
+        if k in head:
+            line[k] = head[k]
+    if world == 1 and not args.no_sub:
+        subs = {}
+        for cfg in (1, 2, 3):
+            if cfg == args.config:
+                continue
+            try:
+                r = single_leg(cfg, args, torch, flush, local, world, max(3, args.steps // 2), max(3, args.warmup),
+                               full=True)
+                r.pop("config", None)
+                subs[W.SINGLE[cfg]["name"]] = r
+            except SystemExit as e:
+                subs[W.SINGLE[cfg]["name"]] = {"error": str(e)}
+        line["single_graph_workloads"] = subs
+    if world == 1 and not args.no_batch:
         try:
-            bl = batched_leg(argparse.Namespace(steps=3, warmup=1), torch, flush, with_cpu=not args.no_cpu)
-            line["batched"] = bl
+            line["batched"] = batched_leg(argparse.Namespace(steps=5, warmup=3), torch, flush,
+                                          with_cpu=not args.no_cpu)
         except Exception as e:   # the single-graph line stands on its own
             line["batched"] = {"error": repr(e)[:200]}
-    if not args.no_serve:
-        try:   # a reduced sample of the served stream (the full one is --config 5)
-            line["served_sample"] = served_leg(60, 2_000_000, False, rates=[200, 800])
+    if world == 1 and not args.no_serve:
+        del flush
+        torch.cuda.empty_cache()
+        try:
+            line["served"] = served_leg(SERVED_REQUESTS, None, True, rates=SERVED_RATES)
         except Exception as e:
-            line["served_sample"] = {"error": repr(e)[:200]}
+            line["served"] = {"error": repr(e)[:200]}
     print(json.dumps(line), flush=True)
 
 

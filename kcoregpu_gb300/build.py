@@ -22,11 +22,16 @@ LIB = PKG / "libkcore_gb300.so"
 CLI = PKG / "kcore"
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_LIB = ORACLE_DIR / "_build" / "libkc_oracle.so"
+ORACLE_SOURCES = ["kc_oracle.c", "kc_gen_oracle.c"]
+ORACLE_CFLAGS = ["-O2", "-std=gnu11", "-fPIC", "-fopenmp", "-ffp-contract=off", "-shared"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Host code is compiled without floating-point contraction: the seeded
+# generators then round every expression the same way on x86 and Arm hosts
+# (Arm compilers would otherwise fuse a*b+c).
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
-                     "-Xcompiler", "-fPIC,-fopenmp,-O3", f"-I{INCLUDE}", f"-I{CSRC}"]
-CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", f"-I{INCLUDE}", f"-I{CSRC}"]
+                     "-Xcompiler", "-fPIC,-fopenmp,-O3,-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 CU_SOURCES = ["kc_peel.cu", "kc_tail.cu", "kc_validate.cu", "kc_api.cu", "kc_noalloc.cu", "kc_batch.cu", "kc_batch_host.cu",
               "kc_serve.cu"]
@@ -93,11 +98,10 @@ def build_library(force: bool = False) -> Path:
 
 
 def build_oracle(force: bool = False) -> Path:
-    src = ORACLE_DIR / "kc_oracle.c"
+    srcs = [ORACLE_DIR / s for s in ORACLE_SOURCES]
     ORACLE_LIB.parent.mkdir(exist_ok=True)
-    if force or _stale(ORACLE_LIB, [src]):
-        _run(["gcc", "-O2", "-std=c11", "-fPIC", "-fopenmp", "-shared", str(src), "-o",
-              str(ORACLE_LIB)])
+    if force or _stale(ORACLE_LIB, srcs):
+        _run(["gcc"] + ORACLE_CFLAGS + [str(s) for s in srcs] + ["-o", str(ORACLE_LIB), "-lm"])
     # driver that replays the reference's host loop around its own kernels
     drv_src = ORACLE_DIR / "ref_peel_driver.cpp"
     drv = ORACLE_DIR / "_build" / "ref_peel_driver"
@@ -110,12 +114,18 @@ def build_oracle(force: bool = False) -> Path:
 
 
 def build_reference_oracle() -> None:
-    """Builds oracle/_ref from the reference sources when they are present
-    (the recipe finds them and exits without building when they are not);
-    elsewhere the prebuilt oracle/_ref files that travel with the tree are used."""
+    """Builds oracle/_ref from the reference sources when a reference checkout
+    is present (KC_REFERENCE_DIR, else a `reference` directory beside this
+    repository); without one nothing is built.  oracle/_ref is git-ignored: its
+    files exist only in a working tree that was built next to the reference
+    sources, and travel with that tree to a GPU host as files (the reference's
+    kernels are a device-code cubin; its x86 loader binary does not run on an
+    Arm host)."""
     script = ORACLE_DIR / "build_ref.sh"
-    if script.exists():
-        subprocess.run(["bash", str(script)], check=False, capture_output=True)
+    ref = os.environ.get("KC_REFERENCE_DIR") or str(ROOT.parent / "reference")
+    if script.exists() and Path(ref, "src").is_dir():
+        subprocess.run(["bash", str(script)], check=False, capture_output=True,
+                       env=dict(os.environ, KC_REFERENCE_DIR=ref))
 
 
 def build_all(force: bool = False) -> None:

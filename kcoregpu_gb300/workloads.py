@@ -66,10 +66,11 @@ SERVED = dict(name="served-poisson-rmat-chunglu+rmat-s24", requests=240, seed_ba
               mmax=8_000_000, big_position=120, big_scale=24, big_edge_factor=16)
 
 
-def served_request(i: int, mmin: int | None = None, mmax: int | None = None):
-    """Request i of the served stream: m ~ log-uniform[10K, 8M] undirected edges,
-    alternating R-MAT (m draws, n = m/8 vertices) and Chung-Lu (gamma ~
-    U[2.1, 2.5], n = m/4, max weight sqrt(n)*8), seed 5000+i -> (offsets, neighbors)."""
+def served_params(i: int, mmin: int | None = None, mmax: int | None = None) -> dict:
+    """Generator parameters of request i of the served stream: m ~
+    log-uniform[10K, 8M] undirected edges, alternating R-MAT (m draws, n = m/8
+    vertices) and Chung-Lu (gamma ~ U[2.1, 2.5], n = m/4, max weight
+    sqrt(n)*8), seed 5000+i."""
     import math
     import numpy as np
     c = SERVED
@@ -78,19 +79,32 @@ def served_request(i: int, mmin: int | None = None, mmax: int | None = None):
     m = int(math.exp(rng.uniform(math.log(lo), math.log(hi))))
     seed = c["seed_base"] + i
     if i % 2 == 0:
-        n = max(64, m // 8)
-        s, t = G.gen_rmat(n, m, seed)
+        return dict(kind="rmat", n=max(64, m // 8), m=m, seed=seed)
+    n = max(64, m // 4)
+    return dict(kind="chung_lu", n=n, m=m, gamma=float(rng.uniform(2.1, 2.5)), max_w=math.sqrt(n) * 8.0, seed=seed)
+
+
+def served_request(i: int, mmin: int | None = None, mmax: int | None = None):
+    """Request i of the served stream (served_params) -> (offsets, neighbors)."""
+    p = served_params(i, mmin, mmax)
+    if p["kind"] == "rmat":
+        s, t = G.gen_rmat(p["n"], p["m"], p["seed"])
     else:
-        n = max(64, m // 4)
-        s, t = G.gen_chung_lu(n, m, float(rng.uniform(2.1, 2.5)), math.sqrt(n) * 8.0, seed)
+        s, t = G.gen_chung_lu(p["n"], p["m"], p["gamma"], p["max_w"], p["seed"])
     off, nbr, _ = G.build_csr(s, t)
     return off, nbr
 
 
-def served_big():
-    """The R-MAT scale-24 edge-factor-16 graph (2^24 vertices, 2^28 draws)."""
+def served_big_params() -> dict:
+    """The R-MAT scale-24 edge-factor-16 graph of the served stream."""
     c = SERVED
     n = 1 << c["big_scale"]
-    s, t = G.gen_rmat(n, n * c["big_edge_factor"], c["seed_base"] + 99999)
+    return dict(kind="rmat", n=n, m=n * c["big_edge_factor"], seed=c["seed_base"] + 99999)
+
+
+def served_big():
+    """The R-MAT scale-24 edge-factor-16 graph (2^24 vertices, 2^28 draws)."""
+    p = served_big_params()
+    s, t = G.gen_rmat(p["n"], p["m"], p["seed"])
     off, nbr, _ = G.build_csr(s, t)
     return off, nbr

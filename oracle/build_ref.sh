@@ -7,9 +7,11 @@
 #   * ref_peel.cubin  : src/ours.cc + src/buffer.cc kernels (selectNodesAtLevel1,
 #                       processNodes1) for sm_103a; oracle/ref_peel_driver.cpp loads it
 #                       through the CUDA driver API on a GPU host
-# Nothing here is copied into the repository.
+# Nothing here is copied into the repository.  The reference tree is taken from
+# KC_REFERENCE_DIR (kcoregpu_gb300/build.py sets it to the checkout beside this
+# repository when one is there).
 set -euo pipefail
-REF=${KC_REFERENCE_DIR:-/root/reference}
+REF=${KC_REFERENCE_DIR:?set KC_REFERENCE_DIR to the reference checkout}
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 [ -d "$REF/src" ] || { echo "reference tree not found at $REF" >&2; exit 1; }

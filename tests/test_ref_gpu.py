@@ -5,8 +5,8 @@ processNodes1, src/ours.cc + src/buffer.cc) are compiled unmodified into
 oracle/_ref/ref_peel.cubin by oracle/build_ref.sh; oracle/ref_peel_driver.cpp
 replays kcore()'s host loop (ours.cc:117-160) through the CUDA driver API and
 writes the final degree array, which is the core numbers.  Our peel must give
-the same core numbers and kmax, bit for bit.  Skipped where the prebuilt
-reference files did not travel with the tree.
+the same core numbers and kmax, bit for bit.  The prebuilt reference cubin must be
+present: a GPU run without it fails here instead of passing quietly.
 """
 import subprocess
 from pathlib import Path
@@ -25,8 +25,8 @@ DRIVER = ROOT / "oracle" / "_build" / "ref_peel_driver"
 
 
 def _reference_peel(off, nbr, tmp: Path):
-    if not CUBIN.exists() or not DRIVER.exists():
-        pytest.skip("the reference's prebuilt kernels are not present")
+    assert CUBIN.exists(), f"the reference's kernels were not built ({CUBIN.name} missing): run oracle/build_ref.sh"
+    assert DRIVER.exists(), f"{DRIVER.name} missing: build the oracle first"
     f = tmp / "csr.bin"
     with open(f, "wb") as fh:
         np.array([len(off) - 1, len(nbr)], np.uint32).tofile(fh)
