@@ -43,6 +43,24 @@ static bool checked_mode() {
 
 static const void* peel_kernel() { return checked_mode() ? peel_persistent_fn_checked() : peel_persistent_fn(); }
 
+const void* peel_kernel_selected() { return peel_kernel(); }
+
+// Longest a device wait may last before the kernel gives up with
+// KC_ERR_TIMEOUT: 2 s.  KC_WAIT_US (read once per process) shortens it for the
+// tests that make a wait run out.
+uint32_t wait_limit_us() {
+    static uint32_t w = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        w = 2000000;
+        if (const char* e = std::getenv("KC_WAIT_US")) {
+            const long long x = std::atoll(e);
+            if (x >= 1 && x <= 60000000) w = (uint32_t)x;
+        }
+    });
+    return w;
+}
+
 // Persistent grid size per device: one CTA per SM (the kernel is compiled for
 // one 512-thread CTA per SM, up to 128 registers a thread).  The late levels
 // are short, and their cost grows with the participants that must arrive at
@@ -132,7 +150,21 @@ void release(kc_graph* g) {
     if (g->own_stream && g->stream) cudaStreamDestroy(g->stream);
 }
 
-uint64_t task_capacity(uint32_t V, uint64_t E) { return (uint64_t)V + E / kChunk + 64; }
+// Task queue entries of a graph: every vertex once plus every hub chunk.
+// KC_TASK_CAP (read once per process) caps it, for the tests that make the
+// queue overflow.
+uint64_t task_capacity(uint32_t V, uint64_t E) {
+    static uint64_t cap = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (const char* e = std::getenv("KC_TASK_CAP")) {
+            const long long x = std::atoll(e);
+            if (x >= 1) cap = (uint64_t)x;
+        }
+    });
+    const uint64_t need = (uint64_t)V + E / kChunk + 64;
+    return cap ? std::min(cap, need) : need;
+}
 
 // Tail hand-off limits: at most KC_TAIL_V survivors (default kTailHandoffV,
 // maximum kTailV; 0 turns the hand-off off) whose induced arcs fit
@@ -380,7 +412,7 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     a.shell_cap = with_order ? g->shell_cap : 0;
     a.max_level = g->maxdeg;
     a.epoch = g->epoch;
-    a.wait_us = 2000000;   // 2 s
+    a.wait_us = wait_limit_us();
     a.E = (uint32_t)g->E;
     a.zero_tasks = 0;   // the queue is cleared by a memset when the tag epoch wraps
     a.alive[0] = g->d_alive[0];

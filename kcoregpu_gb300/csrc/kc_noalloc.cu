@@ -13,7 +13,9 @@
 // The array is shared by every call on a device and keeps the last call's
 // contents; what must start from zero (the level counters, the task queue's
 // tags) is reset by each call.  Calls that overlap on the GPU race on it, so a
-// caller must serialise them (one stream, or wait between calls).
+// caller must serialise them (one stream, or wait between calls); calls from
+// several host threads on one device are serialised here, calls on different
+// devices run independently.
 #include <cstring>
 #include <mutex>
 
@@ -50,6 +52,7 @@ __global__ void noalloc_reset_ctl(PeelCtl* ctl) {
 namespace {
 
 struct DeviceScratch {
+    std::mutex mu;                   // serialises the calls on this device
     bool ready = false;
     unsigned char* base = nullptr;   // device address of g_noalloc_scratch
     uint32_t epoch = 0;              // task-tag epoch of the last call
@@ -57,7 +60,6 @@ struct DeviceScratch {
 };
 
 constexpr int kMaxDevices = 64;
-std::mutex g_na_mu;
 DeviceScratch g_na[kMaxDevices];
 
 // First call on a device: resolve the scratch address (with that device current).
@@ -71,9 +73,13 @@ int noalloc_setup(int dev, DeviceScratch& s) {
     }
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_persistent_fn(), kPeelThreads, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, peel_kernel_selected(), kPeelThreads, 0);
     if (e != cudaSuccess) {
         set_error_msg(std::string("occupancy query: ") + cudaGetErrorString(e));
+        return KC_ERR_CUDA;
+    }
+    if (per < 1 || sms < 1) {   // the cooperative launch needs one resident CTA per SM
+        set_error_msg("kc_peel_noalloc: the peel kernel cannot keep one CTA resident per SM on this device");
         return KC_ERR_CUDA;
     }
     s.base = static_cast<unsigned char*>(p);
@@ -110,8 +116,8 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
         return KC_ERR_NODEV;
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    std::lock_guard<std::mutex> lk(g_na_mu);
     DeviceScratch& s = g_na[dev];
+    std::lock_guard<std::mutex> lk(s.mu);
     int rc = noalloc_setup(dev, s);
     if (rc) return rc;
 
@@ -146,12 +152,12 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
     a.local_budget = kLocalBudget;
     a.claim_cas = 1;   // one graph on the whole GPU
     a.epoch = s.epoch;
-    a.wait_us = 2000000;   // 2 s
+    a.wait_us = wait_limit_us();
     a.E = n_arcs;
     a.alive[0] = reinterpret_cast<uint32_t*>(s.base + kOffAlive0);
     a.alive[1] = reinterpret_cast<uint32_t*>(s.base + kOffAlive1);
     void* args[] = {&a};
-    e = cudaLaunchCooperativeKernel(peel_persistent_fn(), dim3(s.grid), dim3(kPeelThreads), args, 0, st);
+    e = cudaLaunchCooperativeKernel(peel_kernel_selected(), dim3(s.grid), dim3(kPeelThreads), args, 0, st);
     if (e != cudaSuccess) { set_error_msg(std::string("peel launch: ") + cudaGetErrorString(e)); return KC_ERR_CUDA; }
     int err = 0;
     uint32_t kmax = 0;
@@ -163,6 +169,10 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
         set_error_msg("kc_peel_noalloc: invalid CSR (offsets must start at 0 and not decrease, neighbour ids "
                       "must be < V)");
         return KC_ERR_INVALID;
+    }
+    if (err == kErrCheck) {   // bounds-checked kernel (KC_CHECKED=1): an index was out of bounds
+        set_error_msg("kc_peel_noalloc: out-of-bounds index recorded by the checked kernel (access skipped)");
+        return KC_ERR_OVERFLOW;
     }
     if (err) {
         set_error_msg("kc_peel_noalloc: device peel reported an error");

@@ -9,6 +9,12 @@ const void* peel_persistent_fn();
 // Same kernel with every global and shared index bounds-checked (violations are
 // recorded in PeelCtl and skipped); selected with KC_CHECKED=1 in the environment.
 const void* peel_persistent_fn_checked();
+// The persistent kernel the single-graph entry points launch: the
+// bounds-checked one when KC_CHECKED=1 is set in the environment.
+const void* peel_kernel_selected();
+// Time limit (us) of the single-graph peel's device waits (2 s; KC_WAIT_US
+// shortens it for the tests that make a wait run out).
+uint32_t wait_limit_us();
 // One-CTA tail peel (kTailThreads threads, peel_tail_smem() bytes of dynamic
 // shared memory), launched after the persistent kernel on the same stream.
 const void* peel_tail_fn();

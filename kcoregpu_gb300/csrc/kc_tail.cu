@@ -118,9 +118,12 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         while (!(arrived = mbar_try_wait(&s.bar, 0)) && now_ns() - t0 < limit) {}
         if (!__syncthreads_and(arrived)) {
             if (tid == 0) record_error(ctl, kErrTimeout, ctl->tail_level);
-            // the copies may still land: wait for them once more, bounded, before leaving
+            // the copies may still land: wait for them once more before leaving,
+            // bounded by at least 2 s whatever the wait limit (a shortened
+            // limit must not let the CTA exit with its copies in flight)
             const unsigned long long t1 = now_ns();
-            while (!mbar_try_wait(&s.bar, 0) && now_ns() - t1 < limit) {}
+            const unsigned long long drain = limit > 2000000000ull ? limit : 2000000000ull;
+            while (!mbar_try_wait(&s.bar, 0) && now_ns() - t1 < drain) {}
             return;
         }
         for (uint32_t i = tid; i < n; i += kTailThreads) s.st[i] -= s.off[i];

@@ -1,12 +1,23 @@
 // `kcore <edgelist>`: drop-in for the reference CLI (main.cu:44-91) on the
-// GB300 peel.  Prints the same lines for the one variant it runs ("Ours"):
+// GB300 peel.  Prints the reference's lines for the one variant it runs
+// ("Ours"), including the loader's (graph.cpp:13,28,145-152) and the Graph
+// destructor's (graph.cpp:157):
 //
 //   Graph loading Started...
+//   Reading serialized file...                    (cache hit), or
+//   serialized-<file> : File couldn't open        (cache miss)
+//   Reading normal file...
+//   [serialized-<file> : File couldn't open]      (the cache could not be written)
+//   File Loaded in: <ms>
 //   ******************  <file> ******************
 //   V: <V>
 //   E: <arcs>
 //   Ours: <ms>
 //   Kmax: <kmax>
+//   Deallocated...
+//
+// A text file that cannot be opened prints "load graph file failed " and exits
+// with status 255, like graph.cpp:63-66's exit(-1).
 //
 // Options (after the file): --cache-dir DIR (default ./output/, the reference's
 // OUTPUT_LOC), --parse reference|snap, --json (writes DIR/pkc-kcore-<file>,
@@ -14,6 +25,7 @@
 // k-shell offsets), --stats (one JSON line with device timing).
 #include <chrono>
 #include <cstdio>
+#include <sys/stat.h>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -45,14 +57,31 @@ int main(int argc, char** argv) {
         else { std::fprintf(stderr, "unknown option %s\n", a.c_str()); return 2; }
     }
     std::printf("Graph loading Started... \n");
+    const std::string base = ds.substr(ds.find_last_of('/') + 1);
+    std::string cdir = cache;
+    if (!cdir.empty() && cdir.back() != '/') cdir.push_back('/');
     kc_csr_host g{};
     int from_cache = 0;
     auto t0 = std::chrono::steady_clock::now();
     int rc = kc_load_graph(ds.c_str(), cache.c_str(), mode, &g, &from_cache);
+    if (rc == KC_ERR_IO) {   // graph.cpp:13, 145, 63-66
+        std::printf("serialized-%s : File couldn't open\n", base.c_str());
+        std::printf("Reading normal file... \n");
+        std::printf("load graph file failed \n");
+        return 255;
+    }
     if (rc) return die("load", rc);
-    if (!from_cache)
+    if (from_cache) {
+        std::printf("Reading serialized file... \n");   // graph.cpp:13
+    } else {
+        std::printf("serialized-%s : File couldn't open\n", base.c_str());   // graph.cpp:28
+        std::printf("Reading normal file... \n");                           // graph.cpp:145
+        struct stat sb;
+        if (stat((cdir + "serialized-" + base).c_str(), &sb) != 0)          // graph.cpp:52 (cache not written)
+            std::printf("serialized-%s : File couldn't open\n", base.c_str());
         std::printf("File Loaded in: %lld\n", (long long)std::chrono::duration_cast<std::chrono::milliseconds>(
                                                   std::chrono::steady_clock::now() - t0).count());
+    }
     std::printf("******************  %s ****************** \n", ds.c_str());
     std::printf("V: %u\n", g.V);
     std::printf("E: %u\n", g.E);
@@ -73,10 +102,7 @@ int main(int argc, char** argv) {
         std::printf("{\"V\": %u, \"arcs\": %llu, \"kmax\": %u, \"levels\": %u, \"peel_ms\": %.4f, \"blocks\": %u}\n",
                     g.V, (unsigned long long)st.arcs, st.kmax, st.levels, st.peel_ms, st.blocks);
     if (json) {
-        std::string base = ds.substr(ds.find_last_of('/') + 1);
-        std::string d = cache;
-        if (!d.empty() && d.back() != '/') d.push_back('/');
-        rc = kc_write_core_json((d + "pkc-kcore-" + base).c_str(), core.data(), g.V);
+        rc = kc_write_core_json((cdir + "pkc-kcore-" + base).c_str(), core.data(), g.V);
         if (rc) return die("json", rc);
     }
     if (!txt.empty() && (rc = kc_write_core_txt(txt.c_str(), core.data(), g.V))) return die("txt", rc);
@@ -96,5 +122,6 @@ int main(int argc, char** argv) {
     }
     kc_graph_free(dg);
     kc_csr_free(&g);
+    std::printf("Deallocated... \n");   // ~Graph, graph.cpp:157
     return 0;
 }

@@ -132,3 +132,30 @@ def test_malformed_requests_are_refused_and_the_server_continues(gpu, monkeypatc
         assert kmax == wk
         assert t["peel_us"] > 0
     srv.close()
+
+
+@pytest.mark.slow
+def test_served_config_with_the_scale24_graph(gpu):
+    """The served workload's R-MAT scale-24 edge-factor-16 graph (2^24
+    vertices, 2^28 draws, ~407 M undirected edges), bit for bit against BZ:
+    through the server alone, inside a mix of the stream's first requests,
+    and through the one-shot kc_peel_csr."""
+    from kcoregpu_gb300 import workloads as W
+    big = W.served_big()
+    reqs = [W.served_request(i, mmax=2_000_000) for i in range(6)]
+    want_big = O.bz(*big)
+    wants = [O.bz(*r) for r in reqs]
+    srv = Server()
+    core, kmax, t = srv.wait(srv.submit(*big), timeout_s=300)
+    np.testing.assert_array_equal(core, want_big[0])
+    assert kmax == want_big[1]
+    ids = [srv.submit(*r) for r in reqs[:3]] + [srv.submit(*big)] + [srv.submit(*r) for r in reqs[3:]]
+    res = [srv.wait(r, timeout_s=300) for r in ids]
+    srv.close()
+    order = wants[:3] + [want_big] + wants[3:]
+    for (c, k, _), (wc, wk) in zip(res, order):
+        np.testing.assert_array_equal(c, wc)
+        assert k == wk
+    core, kmax = kc.peel_csr(*big)
+    np.testing.assert_array_equal(core, want_big[0])
+    assert kmax == want_big[1]

@@ -6,9 +6,11 @@ for allocation and the device-wide synchronisation it brings).  The test plays
 such a caller: it owns the device buffers (allocated here with torch), hands
 them to the entry point, and checks the core numbers and kmax of two calls in
 a row, on two different graphs, bit for bit against the allocating entry point
-kc_peel_csr.  The second call also shows that the shared scratch is reset
-between calls.  This file sorts last so that a run stopping at its first
-failure has already run every other test.
+kc_peel_csr and against the CPU oracle (Batagelj-Zaversnik).  The second call
+also shows that the shared scratch is reset between calls; a run of 260 calls
+alternating two graphs crosses the 8-bit wrap of the task-tag epoch, after
+which stale queue entries must have been cleared.  This file sorts last so that
+a run stopping at its first failure has already run every other test.
 """
 import ctypes as C
 
@@ -17,6 +19,7 @@ import pytest
 
 import kcoregpu_gb300 as kc
 from kcoregpu_gb300 import _lib
+from oracle import kc_oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -48,6 +51,24 @@ def test_noalloc_matches_allocating_entry_point_on_two_calls(gpu):
         got, gk = _noalloc_peel(torch, off, nbr)
         np.testing.assert_array_equal(got, want)
         assert gk == wk
+        bz, bk = O.bz(off, nbr)
+        np.testing.assert_array_equal(got, bz)
+        assert gk == bk
+
+
+def test_noalloc_across_the_task_tag_wrap(gpu):
+    # 260 calls alternating two graphs with hubs (queued tasks every call): the
+    # calls just after the 255th reuse the queue with the tag epoch wrapped.
+    torch = pytest.importorskip("torch")
+    graphs = [kc.build_csr(*kc.gen_chung_lu(8_000, 40_000, 2.1, 2_000.0, seed=31))[:2],
+              kc.build_csr(*kc.gen_rmat(6_000, 50_000, seed=32))[:2]]
+    wants = [O.bz(off, nbr) for off, nbr in graphs]
+    for i in range(260):
+        off, nbr = graphs[i % 2]
+        got, gk = _noalloc_peel(torch, off, nbr)
+        want, wk = wants[i % 2]
+        assert gk == wk, f"call {i}"
+        np.testing.assert_array_equal(got, want, err_msg=f"call {i}")
 
 
 def test_noalloc_rejects_graphs_beyond_its_limit(gpu):
