@@ -8,7 +8,8 @@ once at start-up.
   the reference would spin in `while(count < V)`, src/ours.cc:138), and the
   same process then peels a batch bit for bit (the context stays usable).  A
   fresh process with the default limit peels the path bit for bit.
-* KC_TASK_CAP=8 leaves the task queue room for 8 entries: a graph with hubs
+* KC_TASK_CAP=8 leaves the task queue room for 8 entries: a 200,000-leaf
+  star, whose hub is claimed in level 1 and queues its adjacency as 782 tasks,
   returns KC_ERR_OVERFLOW (where the reference's queue overflow is an assert
   trap, src/buffer.cc:2), and the process again peels a batch bit for bit.
 * KC_CHECKED=1 runs the bounds-checked kernel (every global and shared index
@@ -77,7 +78,8 @@ def test_a_wait_that_runs_out_returns_timeout(gpu):
 
 
 def test_a_full_task_queue_returns_overflow(gpu):
-    code = ("off, nbr = kc.build_csr(*kc.gen_chung_lu(200_000, 1_000_000, 2.1, 20_000.0, seed=9))[:2]\n"
+    code = ("s = np.zeros(200_000, np.uint32); t = np.arange(1, 200_001, dtype=np.uint32)\n"
+            "off, nbr = kc.build_csr(s, t)[:2]\n"
             "print(json.dumps({'hubs': try_peel(off, nbr), 'batch': batch_ok()}))")
     assert _child(code, KC_TASK_CAP=8) == {"hubs": "KC_ERR_OVERFLOW", "batch": True}
 
