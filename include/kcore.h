@@ -166,6 +166,19 @@ int  kc_graph_device_ptrs(kc_graph* g, const uint32_t** d_offsets,
                           const uint32_t** d_neighbors, uint32_t** d_core);
 void kc_graph_free(kc_graph* g);
 
+/* The autotuner's settings for a graph (no reference counterpart; the
+ * reference's are compile-time constants, inc/common.h:4-12).  Chosen at upload
+ * (kc_graph_upload, kc_peel_csr) from the degree distribution sampled from the
+ * host offsets; none of them changes a result.                                 */
+typedef struct kc_tuning {
+    uint32_t hub_arcs;       /* vertices with more arcs are split into queued tasks  */
+    uint32_t chunk_arcs;     /* arcs per queued task (64..256)                       */
+    uint32_t local_budget;   /* arcs a warp's cascade list holds before queueing     */
+    uint32_t tail_v;         /* survivors at which the one-CTA tail takes over (0: never) */
+    uint32_t grid;           /* persistent CTAs (0: one per SM)                      */
+} kc_tuning;
+int  kc_autotune(const uint32_t* offsets, uint32_t V, kc_tuning* out);
+
 /* One-shot: host CSR in, host core numbers out (cached device buffers per
  * device; pinned host arrays upload fastest).  The CSR is checked on the device
  * after the upload, before the peel reads it (KC_ERR_INVALID).  kmax as the

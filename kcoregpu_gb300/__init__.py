@@ -6,7 +6,7 @@ peel raises KCoreError(KC_ERR_NODEV) when no device is present.
 """
 from ._lib import KCoreError, lib  # noqa: F401
 from .graph import (  # noqa: F401
-    DeviceGraph, Graph, build_csr, device_info, gen_chung_lu, gen_er, gen_rmat, kcore,
+    DeviceGraph, Graph, autotune, build_csr, device_info, gen_chung_lu, gen_er, gen_rmat, kcore,
     load_edgelist, peel_csr, read_csr_binary, read_serialized, write_core_json, write_core_txt,
     write_csr_binary, write_edgelist, write_serialized,
 )

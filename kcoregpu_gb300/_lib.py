@@ -78,6 +78,14 @@ class ServeStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Tuning(C.Structure):
+    _fields_ = [("hub_arcs", C.c_uint32), ("chunk_arcs", C.c_uint32), ("local_budget", C.c_uint32),
+                ("tail_v", C.c_uint32), ("grid", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class BatchStats(C.Structure):
     _fields_ = [("ngraphs", C.c_uint32), ("giants", C.c_uint32), ("blocks", C.c_uint32),
                 ("qcap", C.c_uint32), ("V_total", C.c_uint64), ("arcs_total", C.c_uint64),
@@ -119,6 +127,7 @@ SIGNATURES = {
     "kc_graph_device_ptrs": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp)]),
     "kc_graph_free": (None, [_vp]),
     "kc_peel_csr": (C.c_int, [_u32p, _u32p, C.c_uint32, _u32p, _u32p]),
+    "kc_autotune": (C.c_int, [_u32p, C.c_uint32, C.POINTER(Tuning)]),
     "kc_peel_noalloc": (C.c_int, [_vp, _vp, C.c_uint32, C.c_uint32, _vp, _u32p, _vp]),
     "kc_batch_upload": (C.c_int, [C.POINTER(SegCsr), C.POINTER(_vp)]),
     "kc_batch_set_stream": (C.c_int, [_vp, _vp]),

@@ -91,6 +91,7 @@ static int persistent_grid(int dev) {
 using namespace kc;
 
 struct kc_graph {
+    kc_tuning tune{};       // settings the autotuner chose at upload
     int dev = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
@@ -162,25 +163,8 @@ uint64_t task_capacity(uint32_t V, uint64_t E) {
             if (x >= 1) cap = (uint64_t)x;
         }
     });
-    const uint64_t need = (uint64_t)V + E / kChunk + 64;
+    const uint64_t need = (uint64_t)V + E / kMinChunk + 64;   // (the smallest chunk a launch may choose)
     return cap ? std::min(cap, need) : need;
-}
-
-// Tail hand-off limits: at most KC_TAIL_V survivors (default kTailHandoffV,
-// maximum kTailV; 0 turns the hand-off off) whose induced arcs fit
-// KC_TAIL_ARCS (default kTailArcs).
-void tail_limits(uint32_t* cap_v, uint32_t* cap_arcs) {
-    static uint32_t v = 0, arcs = 0;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        v = kTailHandoffV;
-        arcs = kTailArcs;
-        if (const char* e = std::getenv("KC_TAIL_V")) v = (uint32_t)std::min<long long>(std::max(0ll, std::atoll(e)), kTailV);
-        if (const char* e = std::getenv("KC_TAIL_ARCS"))
-            arcs = (uint32_t)std::min<long long>(std::max(1ll, std::atoll(e)), 1ll << 30);
-    });
-    *cap_v = v;
-    *cap_arcs = arcs;
 }
 
 // Walk mode of the one-graph peel: claim by CAS without reading the state
@@ -194,26 +178,61 @@ uint32_t claim_cas() {
     return c;
 }
 
-// Arcs a warp's cascade list may hold before the rest of a cascade is queued
-// for other warps (KC_LOCAL_BUDGET, default kLocalBudget).
-uint32_t local_budget() {
-    static uint32_t b = 0;
+// Experiment overrides of the tuned settings, read once per process (unset:
+// the autotuner decides).  None changes a result.
+struct Overrides {
+    long long hub_arcs = -1, chunk_arcs = -1, local_budget = -1, tail_v = -1, tail_arcs = -1;
+};
+const Overrides& overrides() {
+    static Overrides o;
     static std::once_flag once;
     std::call_once(once, [] {
-        b = kLocalBudget;
-        if (const char* e = std::getenv("KC_LOCAL_BUDGET")) {
+        auto rd = [](const char* k, long long lo, long long hi) -> long long {
+            const char* e = std::getenv(k);
+            if (!e) return -1;
             const long long x = std::atoll(e);
-            if (x >= 32 && x <= (1 << 20)) b = (uint32_t)x;
-        }
+            return (x >= lo && x <= hi) ? x : -1;
+        };
+        o.hub_arcs = rd("KC_HUB_ARCS", 32, 1 << 20);
+        o.chunk_arcs = rd("KC_CHUNK_ARCS", kMinChunk, kChunk);
+        o.local_budget = rd("KC_LOCAL_BUDGET", 32, 1 << 20);
+        o.tail_v = rd("KC_TAIL_V", 0, kTailV);
+        o.tail_arcs = rd("KC_TAIL_ARCS", 1, 1ll << 30);
     });
-    return b;
+    return o;
 }
 
-// Buffers of the tail hand-off for a graph of at most E arcs.
+// Largest induced adjacency handed to the tail kernel (KC_TAIL_ARCS, default
+// kTailArcs).
+uint32_t tail_arcs_limit() {
+    const long long x = overrides().tail_arcs;
+    return x > 0 ? (uint32_t)x : kTailArcs;
+}
+
+// The autotuner: settings of the single-graph peel from the CSR's degree
+// distribution, sampled from the host offsets in up to 32 runs of 32
+// consecutive vertices (a few KB of reads, so the one-shot call can afford it
+// before its upload), plus V and the arc count.  Experiment overrides win.
+void autotune(const uint32_t* off, uint32_t V, kc_tuning* t) {
+    t->hub_arcs = kLocalArcs;
+    t->chunk_arcs = kChunk;
+    t->local_budget = kLocalBudget;
+    t->tail_v = kTailHandoffV;
+    t->grid = 0;
+    const Overrides& o = overrides();
+    if (o.hub_arcs > 0) t->hub_arcs = (uint32_t)o.hub_arcs;
+    if (o.chunk_arcs > 0) t->chunk_arcs = (uint32_t)o.chunk_arcs;
+    if (o.local_budget > 0) t->local_budget = (uint32_t)o.local_budget;
+    if (o.tail_v >= 0) t->tail_v = (uint32_t)o.tail_v;
+    (void)off; (void)V;
+}
+
+// Buffers of the tail hand-off for a graph of at most E arcs, sized for the
+// largest tail (kTailV survivors); each launch hands over at the tuned point.
 int reserve_tail(kc_graph* g, uint64_t E) {
-    uint32_t cap_v = 0, cap_arcs = 0;
-    tail_limits(&cap_v, &cap_arcs);
-    if (cap_v == 0) { g->tail_cap_v = 0; return KC_OK; }
+    if (overrides().tail_v == 0) { g->tail_cap_v = 0; return KC_OK; }
+    const uint32_t cap_v = kTailV;
+    uint32_t cap_arcs = tail_arcs_limit();
     // room for the padding of every adjacency to a multiple of 4 entries
     cap_arcs = (uint32_t)(((std::min<uint64_t>(cap_arcs, std::max<uint64_t>(E, 1)) + 3ull * kTailV + 16) + 3) & ~3ull);
     const uint64_t items = 2ull * cap_v + E / kFillChunk + 64;
@@ -317,6 +336,7 @@ int graph_create(kc_graph** out) {
 int graph_load(kc_graph* g, const uint32_t* off, const uint32_t* nbr, uint32_t V, bool host_validate = true) {
     const uint64_t E = V ? off[V] : 0;
     if (V && off[0] != 0) { set_error_msg("offsets[0] must be 0"); return KC_ERR_INVALID; }
+    autotune(off, V, &g->tune);
     if (!host_validate) {
         int rc = reserve(g, V, E);
         if (rc) return rc;
@@ -419,11 +439,13 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     a.alive[1] = g->d_alive[1];
     a.trace = with_trace ? g->d_trace : nullptr;
     a.trace_cap = with_trace ? g->trace_cap : 0;
-    a.local_budget = local_budget();
+    a.local_budget = g->tune.local_budget;
+    a.hub_arcs = g->tune.hub_arcs;
+    a.chunk_arcs = g->tune.chunk_arcs;
     a.claim_cas = claim_cas();
-    const bool tail = g->tail_cap_v != 0;
+    const bool tail = g->tail_cap_v != 0 && g->tune.tail_v != 0;
     if (tail) {
-        a.tail_cap_v = g->tail_cap_v;
+        a.tail_cap_v = std::min(g->tail_cap_v, g->tune.tail_v);
         a.tail_cap_arcs = g->tail_cap_arcs;
         a.tail_ids = g->d_tail_ids;
         a.tail_off = g->d_tail_off;
@@ -627,6 +649,12 @@ int kc_peel_csr(const uint32_t* off, const uint32_t* nbr, uint32_t V, uint32_t* 
     if (V) KC_CUDA(cudaMemcpyAsync(core_out, g->d_core, sizeof(uint32_t) * V, cudaMemcpyDeviceToHost, g->stream));
     KC_CUDA(cudaStreamSynchronize(g->stream));
     if (kmax) *kmax = g->h_ctl->kmax;
+    return KC_OK;
+}
+
+int kc_autotune(const uint32_t* offsets, uint32_t V, kc_tuning* out) {
+    if (!out || (V && !offsets)) { set_error_msg("null argument"); return KC_ERR_INVALID; }
+    autotune(offsets, V, out);
     return KC_OK;
 }
 

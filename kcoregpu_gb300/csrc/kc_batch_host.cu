@@ -168,6 +168,8 @@ int launch_single(kc_batch* b, uint32_t g) {
     PeelArgs a;
     std::memset(&a, 0, sizeof(a));
     a.local_budget = kLocalBudget;
+    a.hub_arcs = kLocalArcs;
+    a.chunk_arcs = kChunk;
     a.claim_cas = 1;   // one giant graph on the whole GPU
     a.off = b->d_off + b->vbase[g] + g;
     a.nbr = b->d_nbr + b->abase[g];

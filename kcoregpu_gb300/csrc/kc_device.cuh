@@ -42,8 +42,9 @@ namespace kc {
 constexpr uint32_t kBias = 1u << 30;
 constexpr uint32_t kClaim = 1u << 31;
 constexpr uint32_t kItemCap = 128;    // per-warp batch of arc ranges
-constexpr uint32_t kLocalArcs = 256;  // vertices with more arcs go to the task queue
-constexpr uint32_t kChunk = 256;      // arcs per queued task (len-1 fits 8 bits)
+constexpr uint32_t kLocalArcs = 256;  // default hub threshold: vertices with more arcs go to the task queue
+constexpr uint32_t kChunk = 256;      // largest (and default) arcs per queued task (len-1 fits 8 bits)
+constexpr uint32_t kMinChunk = 64;    // smallest arcs per queued task a launch may choose
 constexpr uint32_t kLocalBudget = 128;   // arcs a warp's cascade list may hold; the rest is queued
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 
@@ -147,6 +148,8 @@ struct PeelArgs {
     uint32_t claim_cas = 0;     // 1: the walk claims by CAS without reading the state first (one graph on
                                 // the whole GPU: latency-bound); 0: it reads the state first (fewer atomics,
                                 // for kernels that peel many graphs at once)
+    uint32_t hub_arcs = kLocalArcs;   // vertices with more arcs are queued as tasks instead of walked inline
+    uint32_t chunk_arcs = kChunk;     // arcs per queued task, kMinChunk..kChunk
 };
 
 // Tail peel: one CTA of kTailThreads threads, states in shared memory.

@@ -150,6 +150,8 @@ extern "C" int kc_peel_noalloc(const uint32_t* d_offsets, const uint32_t* d_neig
     a.V = V;
     a.max_level = kFull;   // from the device validation
     a.local_budget = kLocalBudget;
+    a.hub_arcs = kLocalArcs;
+    a.chunk_arcs = kChunk;
     a.claim_cas = 1;   // one graph on the whole GPU
     a.epoch = s.epoch;
     a.wait_us = wait_limit_us();

@@ -76,10 +76,11 @@ __device__ __forceinline__ void trace(const PeelArgs& a, uint32_t level, int fie
 }
 
 // Pushes the arc range [start, start+len) of every lane with `pred` to the
-// level's task queue, split into chunks of kChunk arcs.
+// level's task queue, split into chunks of a.chunk_arcs arcs.
 __device__ __noinline__ void push_tasks(Warp& w, bool pred, uint32_t start, uint32_t len) {
     const unsigned lane = lane_id();
-    uint32_t nch = pred ? (len + kChunk - 1) / kChunk : 0;
+    const uint32_t ch = w.a.chunk_arcs;
+    uint32_t nch = pred ? (len + ch - 1) / ch : 0;
     uint32_t tot;
     uint32_t ex = warp_excl_scan(nch, &tot);
     if (tot == 0) return;
@@ -98,10 +99,10 @@ __device__ __noinline__ void push_tasks(Warp& w, bool pred, uint32_t start, uint
         const uint32_t s0 = __shfl_sync(kFull, start, src);
         const uint32_t l0 = __shfl_sync(kFull, len, src);
         const uint32_t e0 = __shfl_sync(kFull, ex, src);
-        const uint32_t c0 = (l0 + kChunk - 1) / kChunk;
+        const uint32_t c0 = (l0 + ch - 1) / ch;
         for (uint32_t c = lane; c < c0; c += 32) {
-            const uint32_t cs = s0 + c * kChunk;
-            const uint32_t cl = min(kChunk, l0 - c * kChunk);
+            const uint32_t cs = s0 + c * ch;
+            const uint32_t cl = min(ch, l0 - c * ch);
             if (IN(first + e0 + c, w.a.task_cap, 1))
                 st_relaxed64(&w.a.tasks[first + e0 + c], make_task(cs, cl, w.level, w.a.epoch));
         }
@@ -130,7 +131,7 @@ __device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u, uint
     // The cascade list keeps at most local_budget arcs: the rest of a wide
     // cascade goes to the level's task queue, where idle warps take it,
     // instead of being walked by this warp alone, 128 arcs a step.
-    bool local = found && len <= kLocalArcs;
+    bool local = found && len <= w.a.hub_arcs;
     uint32_t lsum;
     const uint32_t lex = warp_excl_scan(local ? len : 0u, &lsum);
     if (local && w.narcs + lex + len > w.a.local_budget) local = false;
@@ -153,7 +154,7 @@ __device__ __forceinline__ void on_claimed(Warp& w, bool found, uint32_t u, uint
 // later, and the adjacency is read-only while the peel runs.  Hubs go to the
 // task queue, where another SM reads them, and get none.
 __device__ __forceinline__ void prefetch_adjacency(const PeelArgs& a, uint32_t start, uint32_t len) {
-    if (len == 0 || len > kLocalArcs) return;
+    if (len == 0 || len > a.hub_arcs) return;
     asm volatile("prefetch.global.L1 [%0];" ::"l"(a.nbr + start));
     if ((start & 31u) + len > 32u) asm volatile("prefetch.global.L1 [%0];" ::"l"(a.nbr + ((start | 31u) + 1u)));
 }
@@ -320,9 +321,11 @@ __device__ __forceinline__ void walk_items(Warp& w, PendingDec& pd) {
     }
     if (lane == 0) w.b.pref[n] = total;
     __syncwarp();
+    // Neighbour ids of arcs [base, base+128), 4 per lane.  Software-pipelined:
+    // the next step's loads are issued before this step's atomics, so a walk
+    // of more than 128 arcs waits for one neighbour load, not one per step.
     uint32_t lo = 0;
-    for (uint32_t base = 0; base < total; base += 128) {
-        uint32_t u[4];
+    auto load_step = [&](uint32_t base, uint32_t (&u)[4]) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const uint32_t a = base + 32 * j + lane;
@@ -340,6 +343,14 @@ __device__ __forceinline__ void walk_items(Warp& w, PendingDec& pd) {
                 }
             }
         }
+    };
+    uint32_t un[4];
+    load_step(0, un);
+    for (uint32_t base = 0; base < total; base += 128) {
+        uint32_t u[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) u[j] = un[j];
+        if (base + 128 < total) load_step(base + 128, un);
         bool f[4];
         uint32_t cs[4], cl[4];
         if (w.a.claim_cas) {
@@ -402,7 +413,7 @@ __device__ __forceinline__ void stage_claims(Warp& w, const uint32_t (&v)[4], un
             st[j] = s0[j];
             ln[j] = s1[j] - s0[j];
             if (ln[j] == 0) continue;
-            if (ln[j] <= kLocalArcs) localm |= 1u << j; else hubm |= 1u << j;
+            if (ln[j] <= w.a.hub_arcs) localm |= 1u << j; else hubm |= 1u << j;
         }
     }
     const uint32_t cnt = __popc(localm);

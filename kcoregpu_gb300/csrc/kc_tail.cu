@@ -28,10 +28,9 @@ struct TailSmem {
     uint32_t pref[kTailItems + 1];    // quad prefix of the items of one walk round
     uint32_t start[kTailItems];       // first quad of each item
     uint32_t warp_tot[kTailWarps];
+    uint32_t wmin[2][kTailWarps];     // each warp's smallest survivor state, by level parity
     uint32_t qtail;
-    uint32_t minv;
     uint32_t total;
-    uint32_t level_start;             // qtail when the level began (set before the level's barrier)
     unsigned long long bar;           // mbarrier of the bulk copies that stage the offsets and cursors
 };
 static_assert(offsetof(TailSmem, off) % 16 == 0 && offsetof(TailSmem, st) % 16 == 0 &&
@@ -128,46 +127,57 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         }
         for (uint32_t i = tid; i < n; i += kTailThreads) s.st[i] -= s.off[i];
         if (tid == 0) s.qtail = 0;
+        __syncthreads();   // states and the queue end are set before the first scan
     }
 
     bool failed = false;
+    // The queue end at the start of the level; every thread holds the same
+    // value (read before the barrier that closed the previous level).
+    uint32_t lvl_start = 0;
     for (;;) {
-        unsigned long long t_start = 0;
-        if (tid == 0) {
-            s.minv = kFull;
-            s.level_start = s.qtail;
-            if (a.trace) t_start = now_ns();
-        }
-        __syncthreads();
-        // a snapshot taken before the barrier: the scan below appends at once
-        const uint32_t lvl_start = s.level_start;
+        const unsigned long long t_start = (a.trace && tid == 0) ? now_ns() : 0ull;
+        const uint32_t par = it & 1u;
         // scan: every vertex whose degree equals the level (ours.cc:15-25);
-        // peeled vertices keep the level they were peeled at, below this one
-        uint32_t mymin = kFull;
-        // 16-byte reads of 4 states; the loop bound is warp-uniform
-        for (uint32_t b0 = (tid >> 5) * 128; b0 < n; b0 += 4 * kTailThreads) {
-            const uint32_t b = b0 + 4 * lane;
-            const uint4 x = b < n ? *reinterpret_cast<const uint4*>(s.st + b) : make_uint4(0, 0, 0, 0);
-            const uint32_t d[4] = {x.x, x.y, x.z, x.w};
-            unsigned hit = 0;
+        // peeled vertices keep the level they were peeled at, below this one.
+        // 16-byte reads of 4 states, up to 4 groups per lane with their loads
+        // in flight together, and one warp-aggregated append for all of them
+        // (a shared-memory atomic on one word costs ~30 cycles per warp, in
+        // series).  The smallest survivor state is kept per warp, with no
+        // atomic: only a level that peels nothing needs it.
+        uint32_t mymin = kFull, hit = 0;
+        {
+            const uint32_t wb = (tid >> 5) * 128 + 4 * lane;
+            uint4 x[kTailV / (4 * kTailThreads)];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                if (b + k < n && d[k] > level) mymin = min(mymin, d[k]);
-                if (b + k < n && d[k] == level) hit |= 1u << k;
+            for (uint32_t r = 0; r < kTailV / (4 * kTailThreads); ++r) {
+                const uint32_t b = wb + r * 4 * kTailThreads;
+                x[r] = b < n ? *reinterpret_cast<const uint4*>(s.st + b) : make_uint4(0, 0, 0, 0);
             }
-            if (__any_sync(kFull, hit != 0)) {   // one warp-aggregated append for the 4 states
+#pragma unroll
+            for (uint32_t r = 0; r < kTailV / (4 * kTailThreads); ++r) {
+                const uint32_t b = wb + r * 4 * kTailThreads;
+                const uint32_t d[4] = {x[r].x, x[r].y, x[r].z, x[r].w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if (b + k < n && d[k] > level) mymin = min(mymin, d[k]);
+                    if (b + k < n && d[k] == level) hit |= 1u << (4 * r + k);
+                }
+            }
+            if (__any_sync(kFull, hit != 0)) {
                 uint32_t htot;
                 const uint32_t hex = warp_excl_scan(__popc(hit), &htot);
                 uint32_t pos = 0;
                 if (lane == 0) pos = atomicAdd(&s.qtail, htot);
                 pos = __shfl_sync(kFull, pos, 0) + hex;
-#pragma unroll
-                for (int k = 0; k < 4; ++k)
-                    if ((hit >> k) & 1u) { if (pos < kTailV) s.q[pos] = b + k; ++pos; }
+                for (uint32_t m = hit; m; m &= m - 1u) {
+                    const uint32_t bit = __ffs(m) - 1;
+                    if (pos < kTailV) s.q[pos] = wb + (bit >> 2) * 4 * kTailThreads + (bit & 3u);
+                    ++pos;
+                }
             }
         }
         mymin = __reduce_min_sync(kFull, mymin);
-        if (lane == 0 && mymin != kFull) atomicMin(&s.minv, mymin);
+        if (lane == 0) s.wmin[par][tid >> 5] = mymin;
         __syncthreads();
 
         // walk rounds over the queue, including the vertices the walk itself
@@ -290,8 +300,11 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         // A level that peeled nothing changed no degree: jump to the smallest
         // survivor degree (every level in between is empty).
         uint32_t next = level + 1;
-        const uint32_t mn = s.minv;
-        if (tail == lvl_start && mn != kFull && mn > next) next = mn;
+        if (tail == lvl_start) {
+            uint32_t mn = kFull;
+            for (uint32_t w = 0; w < kTailWarps; ++w) mn = min(mn, s.wmin[par][w]);
+            if (mn != kFull && mn > next) next = mn;
+        }
         if (next > max_level) {   // cannot happen for a valid CSR: every vertex is peeled by its degree
             if (tid == 0) record_error(ctl, kErrOverflow, level);
             failed = true;
@@ -300,7 +313,8 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         if (tid == 0 && a.shells)
             for (uint32_t l = level + 2; l <= next && l < a.shell_cap; ++l) a.shells[l] = peeled;
         level = next;
-        __syncthreads();   // every thread has read minv and qtail
+        lvl_start = tail;
+        __syncthreads();   // every thread has read the queue end and the minima
     }
     if (failed) return;
     // Outputs: the state of a peeled vertex is its core number; the queue is

@@ -106,6 +106,15 @@ def gen_er(n: int, m: int, seed: int):
     return s, t
 
 
+def autotune(offsets) -> dict:
+    """The autotuner's settings for a CSR (kc_autotune): hub threshold, task
+    chunk, cascade budget, tail hand-off point, grid."""
+    off = u32(offsets)
+    t = L.Tuning()
+    check(lib().kc_autotune(ptr(off), len(off) - 1, C.byref(t)), "kc_autotune")
+    return t.as_dict()
+
+
 def device_info() -> dict:
     sms, grid, ma, mi = C.c_int(), C.c_int(), C.c_int(), C.c_int()
     check(lib().kc_device_info(C.byref(sms), C.byref(grid), C.byref(ma), C.byref(mi)), "kc_device_info")
