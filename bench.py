@@ -502,7 +502,10 @@ def served_leg(requests: int, mmax: int | None, with_big: bool, rates, seed: int
               "max_gang": max(t["gang"] for _, _, t in res)}
         if big_pos is not None:
             pt["big_graph_latency_ms"] = float(lat[big_pos])
-            pt["big_graph_peel_ms"] = res[big_pos][2]["peel_us"] / 1e3
+            bt = res[big_pos][2]
+            pt["big_graph_peel_ms"] = bt["peel_us"] / 1e3
+            pt["big_graph_parts_ms"] = {"queue": bt["queue_us"] / 1e3, "copy_in": bt["copy_in_us"] / 1e3,
+                                        "copy_out": bt["copy_out_us"] / 1e3}
         sweep.append(pt)
         del res
     st = srv.stats()

@@ -3,6 +3,7 @@
 // Replaces the reference's kcore() host loop (src/ours.cc:117-160) and its
 // device memory glue (src/gpu_memory_allocation.cu:4-22).
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -210,21 +211,52 @@ uint32_t tail_arcs_limit() {
 }
 
 // The autotuner: settings of the single-graph peel from the CSR's degree
-// distribution, sampled from the host offsets in up to 32 runs of 32
-// consecutive vertices (a few KB of reads, so the one-shot call can afford it
-// before its upload), plus V and the arc count.  Experiment overrides win.
+// distribution, sampled from the host offsets in 32 runs of 32 consecutive
+// vertices (a few KB of reads, so the one-shot call can afford it before its
+// upload), plus V.  The rules come from one-at-a-time sweeps on GB300 over
+// R-MAT (400K, 2^20, 2^22 vertices), Chung-Lu (gamma 2.1 and 2.5) and
+// Erdos-Renyi graphs:
+//  * task chunks of 64 arcs: hubs split finer cost nothing where there are
+//    none and gained 1-13% where there are (R-MAT 2^22: 7.18 -> 6.27 ms);
+//  * the cascade budget follows the spread of the degrees: near-uniform degrees
+//    (coefficient of variation below 1) gain from long warp-local cascades
+//    (512 arcs: Erdos-Renyi 1M -12%), skewed ones lose (R-MAT 400K +8%), and
+//    skewed graphs above 2M vertices sit between (256);
+//  * the one-CTA tail takes the last 16,384 survivors of a graph above 256K
+//    vertices (-1.6% on R-MAT 400K, -0.8% on Chung-Lu 2.4M), 12,288 below;
+//  * the hub threshold moved nothing by more than 1% between 128 and 1,024
+//    arcs and stays 256.
+// Experiment overrides win.
 void autotune(const uint32_t* off, uint32_t V, kc_tuning* t) {
     t->hub_arcs = kLocalArcs;
-    t->chunk_arcs = kChunk;
+    t->chunk_arcs = kMinChunk;
     t->local_budget = kLocalBudget;
     t->tail_v = kTailHandoffV;
     t->grid = 0;
+    if (V && off) {
+        constexpr uint32_t kRuns = 32, kRun = 32;
+        double sum = 0, sq = 0;
+        uint32_t cnt = 0;
+        for (uint32_t r = 0; r < kRuns; ++r) {
+            const uint64_t v0 = (uint64_t)V * r / kRuns;
+            for (uint32_t i = 0; i < kRun && v0 + i < V; ++i) {
+                const double d = (double)(off[v0 + i + 1] - off[v0 + i]);
+                sum += d;
+                sq += d * d;
+                ++cnt;
+            }
+        }
+        const double mean = sum / cnt;
+        const double var = sq / cnt - mean * mean;
+        const double cv = mean > 0 ? std::sqrt(var > 0 ? var : 0.0) / mean : 0.0;
+        t->local_budget = cv < 1.0 ? 512u : (V >= (2u << 20) ? 256u : kLocalBudget);
+        t->tail_v = V > (256u << 10) ? kTailV : kTailHandoffV;
+    }
     const Overrides& o = overrides();
     if (o.hub_arcs > 0) t->hub_arcs = (uint32_t)o.hub_arcs;
     if (o.chunk_arcs > 0) t->chunk_arcs = (uint32_t)o.chunk_arcs;
     if (o.local_budget > 0) t->local_budget = (uint32_t)o.local_budget;
     if (o.tail_v >= 0) t->tail_v = (uint32_t)o.tail_v;
-    (void)off; (void)V;
 }
 
 // Buffers of the tail hand-off for a graph of at most E arcs, sized for the

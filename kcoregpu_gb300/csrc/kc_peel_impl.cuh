@@ -321,9 +321,9 @@ __device__ __forceinline__ void walk_items(Warp& w, PendingDec& pd) {
     }
     if (lane == 0) w.b.pref[n] = total;
     __syncwarp();
-    // Neighbour ids of arcs [base, base+128), 4 per lane.  Software-pipelined:
-    // the next step's loads are issued before this step's atomics, so a walk
-    // of more than 128 arcs waits for one neighbour load, not one per step.
+    // Neighbour ids of arcs [base, base+128), 4 per lane.  (Issuing the next
+    // step's loads before this step's atomics measured 1-5% slower: it made
+    // the kernel spill registers.)
     uint32_t lo = 0;
     auto load_step = [&](uint32_t base, uint32_t (&u)[4]) {
 #pragma unroll
@@ -344,13 +344,9 @@ __device__ __forceinline__ void walk_items(Warp& w, PendingDec& pd) {
             }
         }
     };
-    uint32_t un[4];
-    load_step(0, un);
     for (uint32_t base = 0; base < total; base += 128) {
         uint32_t u[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) u[j] = un[j];
-        if (base + 128 < total) load_step(base + 128, un);
+        load_step(base, u);
         bool f[4];
         uint32_t cs[4], cl[4];
         if (w.a.claim_cas) {

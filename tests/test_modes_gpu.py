@@ -3,8 +3,9 @@
 The settings are read once per process (KC_CLAIM_CAS: claim by CAS or read
 the state first; KC_TAIL_V: the tail hand-off point, 0 = the persistent
 kernel peels every level; KC_LOCAL_BUDGET: the cascade budget, its minimum
-sending most cascades through the task queue), so each case runs in a fresh
-process.  Every case must give the oracle's core numbers and kmax, through
+sending most cascades through the task queue; KC_HUB_ARCS and KC_CHUNK_ARCS:
+the hub threshold and the task chunk the autotuner otherwise picks), so each
+case runs in a fresh process.  Every case must give the oracle's core numbers and kmax, through
 both the one-shot entry (kc_peel_csr) and a resident graph peeled twice."""
 import os
 import subprocess
@@ -47,8 +48,15 @@ print("ok")
     {"KC_CLAIM_CAS": "0"},
     {"KC_TAIL_V": "0"},
     {"KC_TAIL_V": "16384"},
+    {"KC_TAIL_V": "8192"},
     {"KC_LOCAL_BUDGET": "32"},
+    {"KC_LOCAL_BUDGET": "4096"},
+    {"KC_HUB_ARCS": "32"},
+    {"KC_HUB_ARCS": "4096"},
+    {"KC_CHUNK_ARCS": "256"},
+    {"KC_CHUNK_ARCS": "100"},
     {"KC_CLAIM_CAS": "0", "KC_TAIL_V": "0", "KC_LOCAL_BUDGET": "32"},
+    {"KC_HUB_ARCS": "32", "KC_CHUNK_ARCS": "64", "KC_LOCAL_BUDGET": "32"},
 ], ids=lambda e: ",".join(f"{k}={v}" for k, v in e.items()))
 def test_peel_under_each_setting(gpu, env):
     r = subprocess.run([sys.executable, "-c", CHILD, str(ROOT)], env={**os.environ, **env},
