@@ -354,6 +354,7 @@ struct kc_server {
     size_t bits_bytes = 0;   // its dynamic shared memory per CTA
     cudaStream_t ks = nullptr;     // serve kernel
     cudaStream_t cs = nullptr;     // copies, allocations, publication
+    cudaMemPool_t pool = nullptr;  // the requests' device memory: keeps up to the budget mapped between requests
     ServeCtl* d_ctl = nullptr;
     ServeJob* d_ring = nullptr;
     ServeJob* h_ring = nullptr;    // pinned mirror (copy sources)
@@ -476,16 +477,16 @@ void plan_request(kc_server* s, Request* r) {
 
 int device_alloc(kc_server* s, Request* r) {
     const uint64_t Vpad = (uint64_t)(r->V + 127) / 128 * 128 + 4;
-    KC_CUDA(cudaMallocAsync(&r->d_off, 4 * ((size_t)r->V + 1), s->cs));
-    KC_CUDA(cudaMallocAsync(&r->d_nbr, 4 * std::max<uint64_t>(r->E, 1), s->cs));
-    KC_CUDA(cudaMallocAsync(&r->d_core, 4 * Vpad, s->cs));
+    KC_CUDA(cudaMallocFromPoolAsync(&r->d_off, 4 * ((size_t)r->V + 1), s->pool, s->cs));
+    KC_CUDA(cudaMallocFromPoolAsync(&r->d_nbr, 4 * std::max<uint64_t>(r->E, 1), s->pool, s->cs));
+    KC_CUDA(cudaMallocFromPoolAsync(&r->d_core, 4 * Vpad, s->pool, s->cs));
     if (r->gang > 1) {
-        KC_CUDA(cudaMallocAsync(&r->d_w, 4 * Vpad, s->cs));
-        KC_CUDA(cudaMallocAsync(&r->d_a0, 4 * Vpad, s->cs));
-        KC_CUDA(cudaMallocAsync(&r->d_a1, 4 * Vpad, s->cs));
-        KC_CUDA(cudaMallocAsync(&r->d_tasks, 8 * r->task_cap, s->cs));
-        KC_CUDA(cudaMallocAsync(&r->d_ctl, sizeof(PeelCtl), s->cs));
-        KC_CUDA(cudaMallocAsync(&r->d_fin, 256, s->cs));
+        KC_CUDA(cudaMallocFromPoolAsync(&r->d_w, 4 * Vpad, s->pool, s->cs));
+        KC_CUDA(cudaMallocFromPoolAsync(&r->d_a0, 4 * Vpad, s->pool, s->cs));
+        KC_CUDA(cudaMallocFromPoolAsync(&r->d_a1, 4 * Vpad, s->pool, s->cs));
+        KC_CUDA(cudaMallocFromPoolAsync(&r->d_tasks, 8 * r->task_cap, s->pool, s->cs));
+        KC_CUDA(cudaMallocFromPoolAsync(&r->d_ctl, sizeof(PeelCtl), s->pool, s->cs));
+        KC_CUDA(cudaMallocFromPoolAsync(&r->d_fin, 256, s->pool, s->cs));
         // Resets are copies, never memsets: a memset runs as a kernel and would
         // wait for SM room the serve kernel does not leave.  The task queue is
         // cleared by the gang itself during level 0 (zero_tasks).
@@ -763,6 +764,18 @@ int kc_serve_open(const kc_serve_cfg* cfg, kc_server** out) {
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&s->ks, cudaStreamNonBlocking))) return fail(e, "stream");
     if ((e = cudaStreamCreateWithFlags(&s->cs, cudaStreamNonBlocking))) return fail(e, "stream");
+    {   // A pool of its own that keeps up to the HBM budget mapped: with the
+        // default pool's release threshold of 0, memory freed by one stretch of
+        // requests went back to the system at the next synchronisation, and the
+        // next stretch paid to map it again (a slower first pass).
+        cudaMemPoolProps pp{};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = s->dev;
+        if ((e = cudaMemPoolCreate(&s->pool, &pp))) return fail(e, "memory pool");
+        uint64_t keep = s->cfg.hbm_budget_bytes;
+        if ((e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep))) return fail(e, "memory pool");
+    }
     if ((e = cudaMalloc(&s->d_ctl, sizeof(ServeCtl)))) return fail(e, "ctl");
     if ((e = cudaMemset(s->d_ctl, 0, sizeof(ServeCtl)))) return fail(e, "ctl");
     if ((e = cudaMalloc(&s->d_ring, sizeof(ServeJob) * s->cfg.ring_slots))) return fail(e, "ring");
@@ -980,6 +993,7 @@ int kc_serve_close(kc_server* s) {
     for (auto& ev : s->stage_ev) if (ev) cudaEventDestroy(ev);
     cudaStreamDestroy(s->ks);
     cudaStreamDestroy(s->cs);
+    if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
     return fatal;
 }
