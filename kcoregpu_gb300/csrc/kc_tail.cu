@@ -184,7 +184,12 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
         // appends (same level)
         uint32_t head = lvl_start, tail = min(s.qtail, n);   // each vertex is queued once
         uint32_t rounds = 0, quads = 0;
-        while (head < tail) {
+        // Once every vertex is claimed (queued), the walks still queued can
+        // only decrement peeled vertices, whose state (their core number) is
+        // at or below the level: the reference rule skips those (ours.cc:94),
+        // so they change nothing and are not run.  The final collapse of a
+        // dense core is where this pays.
+        while (head < tail && tail < n) {
             ++rounds;
             const uint32_t m = min(tail - head, kTailItems);
             const uint32_t i0 = 2 * tid, i1 = 2 * tid + 1;
@@ -219,6 +224,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
             uint32_t lo = 0;
             for (uint32_t b = 0; b < total; b += kTailQuads * kTailThreads) {
                 if (b + wq >= total) break;   // warp-uniform
+                if (*(volatile uint32_t*)&s.qtail >= n) break;   // all claimed (see above); one load, warp-uniform
                 uint4 x[kTailQuads];
 #pragma unroll
                 for (int j = 0; j < kTailQuads; ++j) {
