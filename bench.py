@@ -46,7 +46,8 @@ TIMING_NOTE = ("GPU arm: L2 flushed between timed steps (512 MiB write), inputs 
 # one-CTA tail kernel it hands the last levels to -- per workload, from one ncu
 # capture of that workload with the build that is measured here; None where
 # not captured.
-NCU_TRAFFIC = {1: None, 2: 45_338_880 + 3_630_080 + 7_795_712, 3: None}
+NCU_TRAFFIC = {1: 27_792_896 + 837_120 + 11_156_224, 2: 45_363_200 + 3_072_768 + 6_451_968 + 4_608,
+               3: 51_795_968 + 6_880_512 + 5_824_256}
 
 
 def dist_env():
