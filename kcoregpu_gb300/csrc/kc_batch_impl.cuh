@@ -148,9 +148,12 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
 
         // walk rounds over the queue, including vertices appended by the walk
         // itself (same level, ours.cc:60-107)
+        // Once every vertex is queued (claimed), the walks still queued can
+        // only reach peeled vertices, which are never live (ours.cc:94): they
+        // change nothing and are not run.
         uint32_t head = lvl_start;
         uint32_t tail = sh.qtail;
-        while (head < tail) {
+        while (head < tail && tail < V) {
             const uint32_t n = min(tail - head, kBatchChunk);
             uint32_t l0 = 0, l1 = 0, s0 = 0, s1 = 0;
             const uint32_t i0 = 2 * tid, i1 = 2 * tid + 1;
@@ -168,6 +171,7 @@ __device__ void peel_graph_cta(const uint32_t* off, const uint32_t* nb, uint32_t
             constexpr int kWalkArcs = 4;
             uint32_t lo = 0;
             for (uint32_t b = 0; b < total; b += kWalkArcs * kBatchThreads) {
+                if (*(volatile uint32_t*)&sh.qtail >= V) break;   // all claimed (see above)
                 uint32_t u[kWalkArcs];
 #pragma unroll
                 for (int j = 0; j < kWalkArcs; ++j) {
