@@ -127,6 +127,7 @@ typedef struct kc_stats {
     uint64_t tasks;        /* hub chunks / spilled vertices pushed to the queue  */
     float    peel_ms;      /* device time of the peel (CUDA events)              */
     float    total_ms;     /* host wall time of the call                         */
+    uint32_t method;       /* 1: h-index fixed point, 0: level peel              */
 } kc_stats;
 
 typedef struct kc_graph kc_graph;   /* device-resident CSR + peel state         */
@@ -137,6 +138,15 @@ int  kc_graph_upload(const uint32_t* offsets, const uint32_t* neighbors, uint32_
                      kc_graph** g);
 /* Use an existing CUDA stream (cudaStream_t passed as void*; NULL = own stream). */
 int  kc_graph_set_stream(kc_graph* g, void* stream);
+/* Method of this graph's peels: KC_METHOD_AUTO (the process default: the level
+ * peel, or what KC_ALGO=peel|hindex names), KC_METHOD_HINDEX (the h-index fixed
+ * point, with the level peel after KC_HX_ITERS iterations without convergence)
+ * or KC_METHOD_PEEL (the level-synchronous peel).  Same core numbers either
+ * way; kc_stats.method reports which one produced them.                        */
+#define KC_METHOD_AUTO   0
+#define KC_METHOD_HINDEX 1
+#define KC_METHOD_PEEL   2
+int  kc_graph_set_method(kc_graph* g, uint32_t method);
 /* Runs the peel on the device (no host sync).  Results stay on the device.      */
 int  kc_graph_peel_async(kc_graph* g);
 /* Waits for the last peel, copies core numbers (V uint32, may be NULL) and

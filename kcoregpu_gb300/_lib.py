@@ -38,7 +38,7 @@ class CsrHost(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("V", C.c_uint32), ("kmax", C.c_uint32), ("levels", C.c_uint32),
                 ("iterations", C.c_uint32), ("blocks", C.c_uint32), ("arcs", C.c_uint64), ("tasks", C.c_uint64),
-                ("peel_ms", C.c_float), ("total_ms", C.c_float)]
+                ("peel_ms", C.c_float), ("total_ms", C.c_float), ("method", C.c_uint32)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -119,6 +119,7 @@ SIGNATURES = {
     "kc_write_edgelist": (C.c_int, [_cp, _u32p, _u32p, C.c_uint64]),
     "kc_graph_upload": (C.c_int, [_u32p, _u32p, C.c_uint32, C.POINTER(_vp)]),
     "kc_graph_set_stream": (C.c_int, [_vp, _vp]),
+    "kc_graph_set_method": (C.c_int, [_vp, C.c_uint32]),
     "kc_graph_peel_async": (C.c_int, [_vp]),
     "kc_graph_fetch": (C.c_int, [_vp, _u32p, _u32p, C.POINTER(Stats)]),
     "kc_peel": (C.c_int, [_vp, _u32p, _u32p, C.POINTER(Stats)]),

@@ -131,6 +131,16 @@ struct kc_graph {
     uint32_t* d_tail_cur = nullptr;
     uint32_t* d_tail_nbr = nullptr;
     unsigned long long* d_tail_items = nullptr;
+    // h-index peel (kc_hindex.cu): counts, old estimates, window slots and bins
+    // of large vertices, chunk-task and update-task lists
+    uint32_t* d_hx_cnt = nullptr;
+    uint32_t* d_hx_old = nullptr;
+    HxSlot* d_hx_slots[2] = {nullptr, nullptr};
+    uint32_t* d_hx_bins[2] = {nullptr, nullptr};
+    unsigned long long* d_hx_cl[3] = {nullptr, nullptr, nullptr};
+    unsigned long long* d_hx_bt[2] = {nullptr, nullptr};
+    uint32_t hx_cap_v = 0, hx_cap_l = 0, hx_cap_cl = 0, hx_cap_bt = 0;
+    uint32_t method = KC_METHOD_AUTO;
 };
 
 namespace {
@@ -145,6 +155,9 @@ void release(kc_graph* g) {
     cudaFree(g->d_alive[0]); cudaFree(g->d_alive[1]);
     cudaFree(g->d_tail_ids); cudaFree(g->d_tail_off); cudaFree(g->d_tail_cur); cudaFree(g->d_tail_nbr);
     cudaFree(g->d_tail_items);
+    cudaFree(g->d_hx_cnt); cudaFree(g->d_hx_old);
+    for (int i = 0; i < 2; ++i) { cudaFree(g->d_hx_slots[i]); cudaFree(g->d_hx_bins[i]); cudaFree(g->d_hx_bt[i]); }
+    for (int i = 0; i < 3; ++i) cudaFree(g->d_hx_cl[i]);
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     if (g->h_ctl_init) cudaFreeHost(g->h_ctl_init);
     if (g->ev0) cudaEventDestroy(g->ev0);
@@ -201,6 +214,33 @@ const Overrides& overrides() {
         o.tail_arcs = rd("KC_TAIL_ARCS", 1, 1ll << 30);
     });
     return o;
+}
+
+// Method of the single-graph peel when a graph asks for none: the level peel,
+// or the h-index fixed point (kc_hindex.cu) with the level peel as its
+// fallback when KC_ALGO=hindex (read once per process).
+bool hindex_default() {
+    static bool on = false;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (const char* e = std::getenv("KC_ALGO")) on = std::strcmp(e, "hindex") == 0;
+    });
+    return on;
+}
+
+// Iterations after which the h-index peel gives the graph to the level peel
+// (KC_HX_ITERS, default 256): paths and long chains converge one hop per
+// iteration, where the level peel walks them in one level.
+uint32_t hindex_max_iters() {
+    static uint32_t n = 256;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (const char* e = std::getenv("KC_HX_ITERS")) {
+            const long long x = std::atoll(e);
+            if (x >= 1 && x <= (1 << 24)) n = (uint32_t)x;
+        }
+    });
+    return n;
 }
 
 // Largest induced adjacency handed to the tail kernel (KC_TAIL_ARCS, default
@@ -288,6 +328,43 @@ int reserve_tail(kc_graph* g, uint64_t E) {
         g->tail_items_cap = (uint32_t)items;
     }
     g->tail_cap_v = cap_v;
+    return KC_OK;
+}
+
+// Buffers of the h-index peel for the graph's capacity.  Large vertices (more
+// than kHxWarpArcs arcs) number at most E / (kHxWarpArcs + 1); a pass queues at
+// most one chunk task per kHxChunk arcs of them plus one per vertex; update
+// tasks are one per vertex plus one per further chunk.
+int reserve_hx(kc_graph* g) {
+    const uint64_t V = g->cap_V, E = g->cap_E;
+    const uint64_t cap_l = E / (kHxWarpArcs + 1) + 1;
+    const uint64_t cap_cl = E / kHxChunk + cap_l + 64;
+    const uint64_t cap_bt = V + E / kHxChunk + 64;
+    if (cap_l > 0xFFFFFFFFull || cap_cl > 0xFFFFFFFFull || cap_bt > 0xFFFFFFFFull) {
+        set_error_msg("graph too large for the h-index peel");
+        return KC_ERR_OVERFLOW;
+    }
+    if (g->d_hx_cnt && g->hx_cap_v >= V && g->hx_cap_l >= cap_l && g->hx_cap_cl >= cap_cl && g->hx_cap_bt >= cap_bt)
+        return KC_OK;
+    cudaFree(g->d_hx_cnt); cudaFree(g->d_hx_old);
+    for (int i = 0; i < 2; ++i) { cudaFree(g->d_hx_slots[i]); cudaFree(g->d_hx_bins[i]); cudaFree(g->d_hx_bt[i]); }
+    for (int i = 0; i < 3; ++i) cudaFree(g->d_hx_cl[i]);
+    g->d_hx_cnt = g->d_hx_old = nullptr;
+    for (int i = 0; i < 2; ++i) { g->d_hx_slots[i] = nullptr; g->d_hx_bins[i] = nullptr; g->d_hx_bt[i] = nullptr; }
+    for (int i = 0; i < 3; ++i) g->d_hx_cl[i] = nullptr;
+    g->hx_cap_v = 0;
+    KC_CUDA(cudaMalloc(&g->d_hx_cnt, sizeof(uint32_t) * (V + 4)));
+    KC_CUDA(cudaMalloc(&g->d_hx_old, sizeof(uint32_t) * (V + 4)));
+    for (int i = 0; i < 2; ++i) {
+        KC_CUDA(cudaMalloc(&g->d_hx_slots[i], sizeof(HxSlot) * cap_l));
+        KC_CUDA(cudaMalloc(&g->d_hx_bins[i], sizeof(uint32_t) * kHxBinWords * cap_l));
+        KC_CUDA(cudaMalloc(&g->d_hx_bt[i], sizeof(unsigned long long) * cap_bt));
+    }
+    for (int i = 0; i < 3; ++i) KC_CUDA(cudaMalloc(&g->d_hx_cl[i], sizeof(unsigned long long) * cap_cl));
+    g->hx_cap_v = (uint32_t)V;
+    g->hx_cap_l = (uint32_t)cap_l;
+    g->hx_cap_cl = (uint32_t)cap_cl;
+    g->hx_cap_bt = (uint32_t)cap_bt;
     return KC_OK;
 }
 
@@ -486,6 +563,35 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         a.tail_items = g->d_tail_items;
         a.tail_items_cap = g->tail_items_cap;
     }
+    // The h-index peel first (not for the peel order, the per-level trace or the
+    // bounds-checked build, which follow the level peel); the persistent kernel
+    // returns at once when it solved the graph.
+    const bool hindex = g->method == KC_METHOD_HINDEX || (g->method == KC_METHOD_AUTO && hindex_default());
+    if (hindex && !with_order && !with_trace && !checked_mode()) {
+        int rc = reserve_hx(g);
+        if (rc) return rc;
+        HxArgs h;
+        h.off = g->d_off;
+        h.nbr = g->d_nbr;
+        h.est = g->d_core;
+        h.cnt = g->d_hx_cnt;
+        h.old = g->d_hx_old;
+        h.rm[0] = g->d_alive[0];
+        h.rm[1] = g->d_alive[1];
+        for (int i = 0; i < 2; ++i) { h.slots[i] = g->d_hx_slots[i]; h.bins[i] = g->d_hx_bins[i]; h.bt[i] = g->d_hx_bt[i]; }
+        for (int i = 0; i < 3; ++i) h.cl[i] = g->d_hx_cl[i];
+        h.ctl = g->d_ctl;
+        h.V = g->V;
+        h.E = (uint32_t)g->E;
+        h.cap_l = g->hx_cap_l;
+        h.cap_cl = g->hx_cap_cl;
+        h.cap_bt = g->hx_cap_bt;
+        h.max_iters = hindex_max_iters();
+        h.wait_us = wait_limit_us();
+        h.max_level = g->maxdeg;
+        void* hargs[] = {&h};
+        KC_CUDA(cudaLaunchCooperativeKernel(peel_hindex_fn(), dim3(g->grid), dim3(kPeelThreads), hargs, 0, g->stream));
+    }
     void* args[] = {&a};
     KC_CUDA(cudaLaunchCooperativeKernel(peel_kernel(), dim3(g->grid), dim3(kPeelThreads), args, 0, g->stream));
     if (tail)
@@ -520,11 +626,12 @@ int graph_finish(kc_graph* g, kc_stats* st) {
         cudaEventElapsedTime(&ms, g->ev0, g->ev1);
         st->V = g->V;
         st->kmax = g->h_ctl->kmax;
-        st->levels = g->h_ctl->levels;
+        st->levels = g->h_ctl->hx.solved ? g->h_ctl->kmax + 1 : g->h_ctl->levels;
         st->iterations = g->h_ctl->iterations;
         st->blocks = (uint32_t)g->grid;
         st->arcs = g->E;
         st->tasks = g->h_ctl->tasks;
+        st->method = g->h_ctl->hx.solved ? 1u : 0u;
         st->peel_ms = ms;
     }
     return KC_OK;
@@ -568,6 +675,12 @@ int kc_graph_upload(const uint32_t* off, const uint32_t* nbr, uint32_t V, kc_gra
     }
     if (rc) { release(g); delete g; return rc; }
     *out = g;
+    return KC_OK;
+}
+
+int kc_graph_set_method(kc_graph* g, uint32_t method) {
+    if (!g || method > KC_METHOD_PEEL) { set_error_msg("unknown method"); return KC_ERR_INVALID; }
+    g->method = method;
     return KC_OK;
 }
 

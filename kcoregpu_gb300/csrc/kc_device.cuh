@@ -82,6 +82,25 @@ struct alignas(128) LevelSlot {
     unsigned int pad3[28];
 };
 
+// Control words of the h-index peel (kc_hindex.cu).  Work lists come in
+// rotating copies so that no counter is cleared while a producer of the same
+// sub-phase may add to it: chunk-task lists by sub-phase mod 3, the others by
+// iteration parity.  Each hot counter has its own 128-byte line.
+struct alignas(128) HxCtl {
+    unsigned int solved;       // 1: every core number is found (the peel kernels return at once)
+    unsigned int iters;        // h-index iterations run
+    unsigned int passes;       // window passes over large vertices (sub-phases of phase A)
+    unsigned int pad0[29];
+    unsigned int cl_n[3];      // chunk tasks of large vertices, by sub-phase mod 3
+    unsigned int pad1[29];
+    unsigned int bt_n[2];      // update tasks (vertices whose estimate dropped), by iteration parity
+    unsigned int pad2[30];
+    unsigned int rm_n[2];      // next frontier: vertices of at most kHxWarpArcs arcs
+    unsigned int pad3[30];
+    unsigned int rl_n[2];      // next frontier: larger vertices (window slots)
+    unsigned int pad4[30];
+};
+
 struct alignas(128) PeelCtl {
     LevelSlot slot[4];
     unsigned int iters_done;   // level iterations completed (CTA 0 writes it; diagnostics)
@@ -106,6 +125,46 @@ struct alignas(128) PeelCtl {
     unsigned int tail_arcs;    // arcs of the induced CSR
     unsigned int maxdeg;       // maximum degree found by the device-side CSR validation
     unsigned int pad2[13];
+    HxCtl hx;                  // h-index peel (zero when only the level peel runs)
+};
+
+// h-index peel of one graph (kc_hindex.cu).
+constexpr uint32_t kHxLaneArcs = 16;    // iteration 1: one lane finds the h-index of a vertex this small
+constexpr uint32_t kHxWarpArcs = 256;   // one warp, 8 values a lane; larger vertices are split in chunks
+constexpr uint32_t kHxChunk = 256;      // arcs per chunk task
+constexpr uint32_t kHxBinWords = 40;    // per window slot: 32 bins, the count above the window, padding
+
+// Window state of a large vertex whose h-index is being searched.  Bin b
+// counts the neighbour estimates in [lo + b*2^sh, lo + (b+1)*2^sh - 1]
+// (clipped at hi); bin 32 counts those above hi.
+struct HxSlot {
+    uint32_t v;       // vertex
+    uint32_t e;       // its estimate when the search started (upper bound of the new one)
+    uint32_t lo, hi;  // window
+    uint32_t sh;      // log2 of the bin width
+    uint32_t done;    // chunk tasks finished in this pass
+    uint32_t nch;     // chunk tasks per pass
+    uint32_t pad;
+};
+
+struct HxArgs {
+    const uint32_t* off;
+    const uint32_t* nbr;
+    uint32_t* est;      // estimate per vertex; the core number once converged (the core output)
+    uint32_t* cnt;      // neighbours counted at or above the estimate (a lower bound of the true count)
+    uint32_t* old;      // estimate before the last drop
+    uint32_t* rm[2];    // frontier lists of vertices with at most kHxWarpArcs arcs (V each)
+    HxSlot* slots[2];   // frontier of larger vertices, cap_l each
+    uint32_t* bins[2];  // kHxBinWords per slot
+    unsigned long long* cl[3];   // chunk tasks: slot << 32 | chunk
+    unsigned long long* bt[2];   // update tasks: vertex << 32 | chunk
+    PeelCtl* ctl;
+    uint32_t V;
+    uint32_t E;
+    uint32_t cap_l, cap_cl, cap_bt;
+    uint32_t max_iters;   // give up (the level peel runs instead) after this many iterations
+    uint32_t wait_us;
+    uint32_t max_level;   // 0xFFFFFFFF: the CSR was validated on the device (return if that failed)
 };
 
 struct PeelArgs {

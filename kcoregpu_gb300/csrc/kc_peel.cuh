@@ -19,6 +19,10 @@ uint32_t wait_limit_us();
 // shared memory), launched after the persistent kernel on the same stream.
 const void* peel_tail_fn();
 size_t peel_tail_smem();
+// h-index peel (kc_hindex.cu): one cooperative launch of kPeelThreads-thread
+// CTAs, one per SM, launched before the persistent kernel, which returns at
+// once when it set HxCtl::solved.
+const void* peel_hindex_fn();
 // Device-side CSR validation (kc_validate.cu), stream-ordered before a peel
 // launched with max_level = 0xFFFFFFFF; returns 0 or -1 (launch error).
 int launch_validate_csr(const uint32_t* off, const uint32_t* nbr, uint32_t V, uint64_t E, PeelCtl* ctl,

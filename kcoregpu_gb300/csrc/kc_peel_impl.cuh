@@ -1168,6 +1168,8 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
 
 __global__ void __launch_bounds__(kPeelThreads, 1) KC_PEEL_KERNEL(const __grid_constant__ PeelArgs a) {
     __shared__ CtaShared sh;
+    // the h-index peel launched before this kernel found every core number
+    if (ld_relaxed(&a.ctl->hx.solved)) return;
     peel_body(a, sh, blockIdx.x, gridDim.x);
 }
 #endif

@@ -124,7 +124,7 @@ def device_info() -> dict:
 class DeviceGraph:
     """A CSR resident in HBM with its peel state (C ABI kc_graph)."""
 
-    def __init__(self, offsets, neighbors):
+    def __init__(self, offsets, neighbors, method: str = "auto"):
         self.offsets = u32(offsets)
         self.neighbors = u32(neighbors)
         self.V = len(self.offsets) - 1
@@ -132,10 +132,20 @@ class DeviceGraph:
         nb = ptr(self.neighbors) if len(self.neighbors) else None
         check(lib().kc_graph_upload(ptr(self.offsets), nb, self.V, C.byref(h)), "kc_graph_upload")
         self._h = h
+        if method != "auto":
+            self.set_method(method)
 
     @property
     def handle(self):
         return self._h
+
+    METHODS = {"auto": 0, "hindex": 1, "peel": 2}
+
+    def set_method(self, method: str) -> None:
+        """'auto' (the process default), 'hindex' (the h-index fixed point, the
+        level peel after KC_HX_ITERS iterations without convergence) or 'peel'
+        (the level-synchronous peel).  The core numbers are the same."""
+        check(lib().kc_graph_set_method(self._h, self.METHODS[method]), "kc_graph_set_method")
 
     def set_stream(self, stream_handle: int | None) -> None:
         check(lib().kc_graph_set_stream(self._h, C.c_void_p(stream_handle or 0)), "kc_graph_set_stream")

@@ -1,6 +1,8 @@
 """Failure paths of the single-graph peel on the GPU, in forms that fault and
 hang nothing: each runs in a fresh child process with a test-only setting read
-once at start-up.
+once at start-up.  The wait and queue cases are those of the level peel, so
+they run with KC_ALGO=peel (the h-index peel that runs first by default
+solves these graphs without the task queue).
 
 * KC_WAIT_US=50 shortens every device wait of the peel to 50 us.  On a
   300,000-vertex path one warp walks the whole level-1 cascade while the others
@@ -61,7 +63,7 @@ def try_peel(off, nbr):
 
 def _child(code: str, **env) -> dict:
     e = dict(os.environ)
-    for k in ("KC_WAIT_US", "KC_TASK_CAP", "KC_CHECKED"):
+    for k in ("KC_WAIT_US", "KC_TASK_CAP", "KC_CHECKED", "KC_ALGO"):
         e.pop(k, None)
     e.update({k: str(v) for k, v in env.items()})
     r = subprocess.run([sys.executable, "-c", PRELUDE + code], capture_output=True, text=True, timeout=600, env=e,
@@ -71,9 +73,10 @@ def _child(code: str, **env) -> dict:
 
 
 def test_a_wait_that_runs_out_returns_timeout(gpu):
-    out = _child("print(json.dumps({'path': try_peel(*path(300_000)), 'batch': batch_ok()}))", KC_WAIT_US=50)
+    out = _child("print(json.dumps({'path': try_peel(*path(300_000)), 'batch': batch_ok()}))", KC_WAIT_US=50,
+                 KC_ALGO="peel")
     assert out == {"path": "KC_ERR_TIMEOUT", "batch": True}
-    out = _child("print(json.dumps({'path': try_peel(*path(300_000))}))")
+    out = _child("print(json.dumps({'path': try_peel(*path(300_000))}))", KC_ALGO="peel")
     assert out == {"path": "ok"}
 
 
@@ -81,7 +84,7 @@ def test_a_full_task_queue_returns_overflow(gpu):
     code = ("s = np.zeros(200_000, np.uint32); t = np.arange(1, 200_001, dtype=np.uint32)\n"
             "off, nbr = kc.build_csr(s, t)[:2]\n"
             "print(json.dumps({'hubs': try_peel(off, nbr), 'batch': batch_ok()}))")
-    assert _child(code, KC_TASK_CAP=8) == {"hubs": "KC_ERR_OVERFLOW", "batch": True}
+    assert _child(code, KC_TASK_CAP=8, KC_ALGO="peel") == {"hubs": "KC_ERR_OVERFLOW", "batch": True}
 
 
 def test_bounds_checked_kernel_records_no_violation(gpu):

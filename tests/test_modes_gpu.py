@@ -1,5 +1,9 @@
 """GPU parity of the one-graph peel under each of its runtime settings.
 
+The level-peel settings are run with KC_ALGO=peel (the h-index peel, which
+runs first by default, would otherwise solve these graphs before the level
+peel starts); KC_ALGO=hindex runs the h-index peel, and KC_HX_ITERS=3 stops
+it early so that the level peel finishes from scratch.
 The settings are read once per process (KC_CLAIM_CAS: claim by CAS or read
 the state first; KC_TAIL_V: the tail hand-off point, 0 = the persistent
 kernel peels every level; KC_LOCAL_BUDGET: the cascade budget, its minimum
@@ -44,7 +48,7 @@ print("ok")
 """
 
 
-@pytest.mark.parametrize("env", [
+LEVEL_PEEL = [
     {"KC_CLAIM_CAS": "0"},
     {"KC_TAIL_V": "0"},
     {"KC_TAIL_V": "16384"},
@@ -57,7 +61,12 @@ print("ok")
     {"KC_CHUNK_ARCS": "100"},
     {"KC_CLAIM_CAS": "0", "KC_TAIL_V": "0", "KC_LOCAL_BUDGET": "32"},
     {"KC_HUB_ARCS": "32", "KC_CHUNK_ARCS": "64", "KC_LOCAL_BUDGET": "32"},
-], ids=lambda e: ",".join(f"{k}={v}" for k, v in e.items()))
+]
+
+
+@pytest.mark.parametrize("env", [{"KC_ALGO": "peel", **e} for e in LEVEL_PEEL] +
+                         [{"KC_ALGO": "hindex"}, {"KC_ALGO": "hindex", "KC_HX_ITERS": "3"}],
+                         ids=lambda e: ",".join(f"{k}={v}" for k, v in e.items()))
 def test_peel_under_each_setting(gpu, env):
     r = subprocess.run([sys.executable, "-c", CHILD, str(ROOT)], env={**os.environ, **env},
                        capture_output=True, text=True, timeout=600)
