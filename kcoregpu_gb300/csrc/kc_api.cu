@@ -135,9 +135,13 @@ struct kc_graph {
     // of large vertices, chunk-task and update-task lists
     uint32_t* d_hx_cnt = nullptr;
     uint32_t* d_hx_old = nullptr;
+    uint32_t* d_hx_act = nullptr;   // active lists (E), their floors and lengths (V each)
+    uint32_t* d_hx_alo = nullptr;
+    uint32_t* d_hx_alen = nullptr;
     HxSlot* d_hx_slots[2] = {nullptr, nullptr};
     uint32_t* d_hx_bins[2] = {nullptr, nullptr};
     unsigned long long* d_hx_cl[3] = {nullptr, nullptr, nullptr};
+    uint32_t* d_hx_rc[3] = {nullptr, nullptr, nullptr};
     unsigned long long* d_hx_bt[2] = {nullptr, nullptr};
     uint32_t hx_cap_v = 0, hx_cap_l = 0, hx_cap_cl = 0, hx_cap_bt = 0;
     uint32_t method = KC_METHOD_AUTO;
@@ -156,8 +160,9 @@ void release(kc_graph* g) {
     cudaFree(g->d_tail_ids); cudaFree(g->d_tail_off); cudaFree(g->d_tail_cur); cudaFree(g->d_tail_nbr);
     cudaFree(g->d_tail_items);
     cudaFree(g->d_hx_cnt); cudaFree(g->d_hx_old);
+    cudaFree(g->d_hx_act); cudaFree(g->d_hx_alo); cudaFree(g->d_hx_alen);
     for (int i = 0; i < 2; ++i) { cudaFree(g->d_hx_slots[i]); cudaFree(g->d_hx_bins[i]); cudaFree(g->d_hx_bt[i]); }
-    for (int i = 0; i < 3; ++i) cudaFree(g->d_hx_cl[i]);
+    for (int i = 0; i < 3; ++i) { cudaFree(g->d_hx_cl[i]); cudaFree(g->d_hx_rc[i]); }
     if (g->h_ctl) cudaFreeHost(g->h_ctl);
     if (g->h_ctl_init) cudaFreeHost(g->h_ctl_init);
     if (g->ev0) cudaEventDestroy(g->ev0);
@@ -334,7 +339,8 @@ int reserve_tail(kc_graph* g, uint64_t E) {
 // Buffers of the h-index peel for the graph's capacity.  Large vertices (more
 // than kHxWarpArcs arcs) number at most E / (kHxWarpArcs + 1); a pass queues at
 // most one chunk task per kHxChunk arcs of them plus one per vertex; update
-// tasks are one per vertex plus one per further chunk.
+// tasks are one per vertex plus one per further chunk; a large vertex's active
+// list lives in its own adjacency's range of an E-word array.
 int reserve_hx(kc_graph* g) {
     const uint64_t V = g->cap_V, E = g->cap_E;
     const uint64_t cap_l = E / (kHxWarpArcs + 1) + 1;
@@ -347,20 +353,27 @@ int reserve_hx(kc_graph* g) {
     if (g->d_hx_cnt && g->hx_cap_v >= V && g->hx_cap_l >= cap_l && g->hx_cap_cl >= cap_cl && g->hx_cap_bt >= cap_bt)
         return KC_OK;
     cudaFree(g->d_hx_cnt); cudaFree(g->d_hx_old);
+    cudaFree(g->d_hx_act); cudaFree(g->d_hx_alo); cudaFree(g->d_hx_alen);
     for (int i = 0; i < 2; ++i) { cudaFree(g->d_hx_slots[i]); cudaFree(g->d_hx_bins[i]); cudaFree(g->d_hx_bt[i]); }
-    for (int i = 0; i < 3; ++i) cudaFree(g->d_hx_cl[i]);
-    g->d_hx_cnt = g->d_hx_old = nullptr;
+    for (int i = 0; i < 3; ++i) { cudaFree(g->d_hx_cl[i]); cudaFree(g->d_hx_rc[i]); }
+    g->d_hx_cnt = g->d_hx_old = g->d_hx_act = g->d_hx_alo = g->d_hx_alen = nullptr;
     for (int i = 0; i < 2; ++i) { g->d_hx_slots[i] = nullptr; g->d_hx_bins[i] = nullptr; g->d_hx_bt[i] = nullptr; }
-    for (int i = 0; i < 3; ++i) g->d_hx_cl[i] = nullptr;
+    for (int i = 0; i < 3; ++i) { g->d_hx_cl[i] = nullptr; g->d_hx_rc[i] = nullptr; }
     g->hx_cap_v = 0;
     KC_CUDA(cudaMalloc(&g->d_hx_cnt, sizeof(uint32_t) * (V + 4)));
     KC_CUDA(cudaMalloc(&g->d_hx_old, sizeof(uint32_t) * (V + 4)));
+    KC_CUDA(cudaMalloc(&g->d_hx_act, sizeof(uint32_t) * (E + 4)));
+    KC_CUDA(cudaMalloc(&g->d_hx_alo, sizeof(uint32_t) * (V + 4)));
+    KC_CUDA(cudaMalloc(&g->d_hx_alen, sizeof(uint32_t) * (V + 4)));
     for (int i = 0; i < 2; ++i) {
         KC_CUDA(cudaMalloc(&g->d_hx_slots[i], sizeof(HxSlot) * cap_l));
         KC_CUDA(cudaMalloc(&g->d_hx_bins[i], sizeof(uint32_t) * kHxBinWords * cap_l));
         KC_CUDA(cudaMalloc(&g->d_hx_bt[i], sizeof(unsigned long long) * cap_bt));
     }
-    for (int i = 0; i < 3; ++i) KC_CUDA(cudaMalloc(&g->d_hx_cl[i], sizeof(unsigned long long) * cap_cl));
+    for (int i = 0; i < 3; ++i) {
+        KC_CUDA(cudaMalloc(&g->d_hx_cl[i], sizeof(unsigned long long) * cap_cl));
+        KC_CUDA(cudaMalloc(&g->d_hx_rc[i], sizeof(uint32_t) * cap_l));
+    }
     g->hx_cap_v = (uint32_t)V;
     g->hx_cap_l = (uint32_t)cap_l;
     g->hx_cap_cl = (uint32_t)cap_cl;
@@ -567,7 +580,8 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     // bounds-checked build, which follow the level peel); the persistent kernel
     // returns at once when it solved the graph.
     const bool hindex = g->method == KC_METHOD_HINDEX || (g->method == KC_METHOD_AUTO && hindex_default());
-    if (hindex && !with_order && !with_trace && !checked_mode()) {
+    // (vertex ids below 2^31: the h-index frontier tags entries with the top bit)
+    if (hindex && !with_order && !with_trace && !checked_mode() && g->V < 0x80000000u) {
         int rc = reserve_hx(g);
         if (rc) return rc;
         HxArgs h;
@@ -576,10 +590,13 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         h.est = g->d_core;
         h.cnt = g->d_hx_cnt;
         h.old = g->d_hx_old;
+        h.act = g->d_hx_act;
+        h.alo = g->d_hx_alo;
+        h.alen = g->d_hx_alen;
         h.rm[0] = g->d_alive[0];
         h.rm[1] = g->d_alive[1];
         for (int i = 0; i < 2; ++i) { h.slots[i] = g->d_hx_slots[i]; h.bins[i] = g->d_hx_bins[i]; h.bt[i] = g->d_hx_bt[i]; }
-        for (int i = 0; i < 3; ++i) h.cl[i] = g->d_hx_cl[i];
+        for (int i = 0; i < 3; ++i) { h.cl[i] = g->d_hx_cl[i]; h.rc[i] = g->d_hx_rc[i]; }
         h.ctl = g->d_ctl;
         h.V = g->V;
         h.E = (uint32_t)g->E;

@@ -99,6 +99,10 @@ struct alignas(128) HxCtl {
     unsigned int pad3[30];
     unsigned int rl_n[2];      // next frontier: larger vertices (window slots)
     unsigned int pad4[30];
+    unsigned int bar;          // grid barrier: arrivals so far (barrier k completes at k * grid)
+    unsigned int pad5[31];
+    unsigned int rc_n[3];      // CTA entries (large vertices read whole by one CTA), by sub-phase mod 3
+    unsigned int pad6[29];
 };
 
 struct alignas(128) PeelCtl {
@@ -133,10 +137,13 @@ constexpr uint32_t kHxLaneArcs = 16;    // iteration 1: one lane finds the h-ind
 constexpr uint32_t kHxWarpArcs = 256;   // one warp, 8 values a lane; larger vertices are split in chunks
 constexpr uint32_t kHxChunk = 256;      // arcs per chunk task
 constexpr uint32_t kHxBinWords = 40;    // per window slot: 32 bins, the count above the window, padding
+constexpr uint32_t kHxCtaVals = 8192;   // a CTA reads a large vertex whole up to this many entries
 
 // Window state of a large vertex whose h-index is being searched.  Bin b
 // counts the neighbour estimates in [lo + b*2^sh, lo + (b+1)*2^sh - 1]
-// (clipped at hi); bin 32 counts those above hi.
+// (clipped at hi); bin 32 counts those above hi.  A pass reads either the
+// whole adjacency (mode 0; it also rebuilds the active list from the
+// neighbours at or above lo) or the vertex's active list (mode 1).
 struct HxSlot {
     uint32_t v;       // vertex
     uint32_t e;       // its estimate when the search started (upper bound of the new one)
@@ -144,7 +151,9 @@ struct HxSlot {
     uint32_t sh;      // log2 of the bin width
     uint32_t done;    // chunk tasks finished in this pass
     uint32_t nch;     // chunk tasks per pass
-    uint32_t pad;
+    uint32_t mode;    // 0: adjacency, 1: active list
+    uint32_t len;     // entries a pass reads
+    uint32_t pad[3];
 };
 
 struct HxArgs {
@@ -153,10 +162,19 @@ struct HxArgs {
     uint32_t* est;      // estimate per vertex; the core number once converged (the core output)
     uint32_t* cnt;      // neighbours counted at or above the estimate (a lower bound of the true count)
     uint32_t* old;      // estimate before the last drop
+    // Active lists of large vertices: act[off[v] ...) holds alen[v] neighbours
+    // of v, every one whose estimate is at or above alo[v] (and possibly some
+    // that fell below since); alen[v] = 0xFFFFFFFF: no list.  Estimates only
+    // fall, so once v's estimate is at or above alo[v] no other neighbour can
+    // count towards its h-index or be crossed by its drops.
+    uint32_t* act;
+    uint32_t* alo;
+    uint32_t* alen;
     uint32_t* rm[2];    // frontier lists of vertices with at most kHxWarpArcs arcs (V each)
     HxSlot* slots[2];   // frontier of larger vertices, cap_l each
     uint32_t* bins[2];  // kHxBinWords per slot
     unsigned long long* cl[3];   // chunk tasks: slot << 32 | chunk
+    uint32_t* rc[3];             // CTA entries: vertex | 0x80000000 when read from its active list
     unsigned long long* bt[2];   // update tasks: vertex << 32 | chunk
     PeelCtl* ctl;
     uint32_t V;

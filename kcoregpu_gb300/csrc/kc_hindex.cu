@@ -60,6 +60,9 @@ namespace {
 constexpr uint32_t kWarps = kPeelThreads / 32;
 constexpr uint32_t kNoBin = 0xFFu;
 constexpr uint32_t kBatchVals = 512;   // neighbour estimates a warp gathers into shared memory at once
+constexpr uint32_t kListTask = 0x80000000u;   // update task flag: scan the active list, not the adjacency
+constexpr uint32_t kListMargin = 32;   // a rebuilt list also keeps neighbours this far below the window
+constexpr uint32_t kListFlag = 0x80000000u;   // warp-frontier entry flag: a large vertex read from its active list
 
 struct HxShared {
     unsigned long long bt_stage[kWarps][32];   // per-warp staging of update tasks
@@ -70,29 +73,31 @@ struct HxShared {
     uint32_t tnew[kWarps][32];
     uint32_t vals[kWarps][kBatchVals];         // phase A: gathered neighbour estimates of a batch
     int bar_ok;
+    unsigned bar_k;   // grid barriers passed (thread 0)
+    uint32_t red[kWarps];   // CTA reductions
+    uint32_t cpos;          // CTA path: active-list append cursor
 };
+static_assert(sizeof(uint32_t) * kWarps * kBatchVals == sizeof(uint32_t) * kHxCtaVals, "the CTA path uses every warp's values");
 
 // Grid barrier of the cooperative launch, bounded in time; false when the wait
-// ran out or an error was recorded (every CTA then returns).
+// ran out or an error was recorded (every CTA then returns).  Arrivals only
+// add to one counter (barrier k is complete at k * grid arrivals), so the
+// last arrival needs no reset and the waiters one load: a fence, an add and
+// the poll are the whole cost.
 __device__ bool hx_barrier(const HxArgs& a, HxShared& sh) {
     __syncthreads();
     if (threadIdx.x == 0) {
         PeelCtl* ctl = a.ctl;
         int ok = 1;
-        const unsigned gen = ld_acquire(&ctl->bar_gen);
+        const unsigned target = ++sh.bar_k * gridDim.x;
         __threadfence();
-        if (atomicAdd(&ctl->bar_count, 1u) == gridDim.x - 1) {
-            atomicExch(&ctl->bar_count, 0u);
-            __threadfence();
-            atomicAdd(&ctl->bar_gen, 1u);
-        } else {
-            const unsigned long long t0 = now_ns(), lim = (unsigned long long)a.wait_us * 1000ull;
-            uint32_t polls = 0;
-            while (ld_acquire(&ctl->bar_gen) == gen) {
-                if ((++polls & 31u) == 0) {
-                    if (ld_err(&ctl->err)) { ok = 0; break; }
-                    if (now_ns() - t0 > lim) { record_error(ctl, kErrTimeout, ctl->hx.iters); ok = 0; break; }
-                }
+        asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;" ::"l"(&ctl->hx.bar) : "memory");
+        const unsigned long long t0 = now_ns(), lim = (unsigned long long)a.wait_us * 1000ull;
+        uint32_t polls = 0;
+        while (ld_acquire(&ctl->hx.bar) < target) {
+            if ((++polls & 31u) == 0) {
+                if (ld_err(&ctl->err)) { ok = 0; break; }
+                if (now_ns() - t0 > lim) { record_error(ctl, kErrTimeout, ctl->hx.iters); ok = 0; break; }
             }
         }
         if (ld_err(&ctl->err)) ok = 0;
@@ -169,95 +174,166 @@ __device__ __forceinline__ uint32_t bin_shift(uint32_t lo, uint32_t hi) {
     return sh;
 }
 
+// Queues the chunk tasks of slot s (pass over `len` entries) for sub-phase r+1.
+__device__ __forceinline__ void queue_chunks(const HxArgs& a, uint32_t r, uint32_t s, uint32_t nch, unsigned lane,
+                                             unsigned step) {
+    HxCtl* hx = &a.ctl->hx;
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&hx->cl_n[(r + 1) % 3], nch);
+    if (step == 32) base = __shfl_sync(kFull, base, 0);
+    if (base + nch > a.cap_cl) {
+        if (lane == 0) record_error(a.ctl, kErrOverflow, 0);
+        return;
+    }
+    for (uint32_t c = lane; c < nch; c += step) a.cl[(r + 1) % 3][base + c] = ((unsigned long long)s << 32) | c;
+}
+
 // One lane opens a window slot for large vertex v (d arcs, estimate e) in the
-// frontier of parity q and queues its chunk tasks for sub-phase r+1.  coarse:
-// the window covers [0, e] (iteration 1, where estimates fall far); otherwise
-// it covers the 32 values at the top, where a drop usually stays.
-__device__ void open_slot(const HxArgs& a, uint32_t q, uint32_t r, uint32_t v, uint32_t e, uint32_t d, bool coarse) {
+// frontier of parity q, searching [lo, hi] in the active list (mode 1, len
+// entries) or the adjacency (mode 0, which rebuilds the list), and queues its
+// chunk tasks for sub-phase r+1.
+__device__ void open_window(const HxArgs& a, uint32_t q, uint32_t r, uint32_t v, uint32_t e, uint32_t lo, uint32_t hi,
+                            uint32_t mode, uint32_t len) {
     HxCtl* hx = &a.ctl->hx;
     const uint32_t s = atomicAdd(&hx->rl_n[q], 1u);
     if (s >= a.cap_l) { record_error(a.ctl, kErrOverflow, 0); return; }
-    const uint32_t nch = (d + kHxChunk - 1) / kHxChunk;
     HxSlot sl;
     sl.v = v;
     sl.e = e;
-    sl.hi = e;
-    sl.lo = coarse ? 0u : (e >= 31u ? e - 31u : 0u);
-    sl.sh = bin_shift(sl.lo, sl.hi);
+    sl.lo = lo;
+    sl.hi = hi;
+    sl.mode = mode;
+    sl.len = len;
+    if (mode == 0) a.alen[v] = 0;   // the pass rebuilds the list
+    sl.sh = bin_shift(lo, hi);
     sl.done = 0;
-    sl.nch = nch;
-    sl.pad = 0;
+    sl.nch = (len + kHxChunk - 1) / kHxChunk;
+    sl.pad[0] = sl.pad[1] = sl.pad[2] = 0;
+    const uint32_t nch = sl.nch;
     a.slots[q][s] = sl;
     uint4* b = reinterpret_cast<uint4*>(a.bins[q] + (size_t)s * kHxBinWords);
 #pragma unroll
     for (int i = 0; i < (int)(kHxBinWords / 4); ++i) b[i] = make_uint4(0, 0, 0, 0);
-    const uint32_t base = atomicAdd(&hx->cl_n[(r + 1) % 3], nch);
-    if (base + nch > a.cap_cl) { record_error(a.ctl, kErrOverflow, 0); return; }
-    unsigned long long* cl = a.cl[(r + 1) % 3];
-    for (uint32_t c = 0; c < nch; ++c) cl[base + c] = ((unsigned long long)s << 32) | c;
+    queue_chunks(a, r, s, nch, 0, 1);
 }
 
-// Largest h in [0, e] with at least h of the warp's values >= h (the values
-// are x[k] of lane l for arc l + 32k < d), and the count at that h.
-__device__ __forceinline__ uint32_t warp_hindex(const uint32_t (&x)[8], uint32_t d, uint32_t e, uint32_t* count) {
-    const unsigned lane = lane_id();
-    uint32_t lo = 0, hi = e;
-    while (lo < hi) {   // warp-uniform
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        uint32_t c = 0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) c += (lane + 32u * k < d && x[k] >= mid) ? 1u : 0u;
-        c = __reduce_add_sync(kFull, c);
-        if (c >= mid) lo = mid; else hi = mid - 1;
+// One lane queues large vertex v (entry flag kListFlag: read its active list)
+// for the CTA path of sub-phase r+1.
+__device__ __forceinline__ void push_cta(const HxArgs& a, uint32_t r, uint32_t ent) {
+    const uint32_t i = atomicAdd(&a.ctl->hx.rc_n[(r + 1) % 3], 1u);
+    if (i < a.cap_l) a.rc[(r + 1) % 3][i] = ent;
+    else record_error(a.ctl, kErrOverflow, 0);
+}
+
+// The window of a large vertex queued for recomputation: its active list from
+// the top 32 values down (when it has one), else the adjacency, from [0, e]
+// when coarse (iteration 1, where estimates fall far) or the top 32 values.
+__device__ void open_slot(const HxArgs& a, uint32_t q, uint32_t r, uint32_t v, uint32_t e, uint32_t d, bool coarse) {
+    const uint32_t al = coarse ? kFull : __ldcg(a.alen + v);
+    const uint32_t l0 = coarse ? 0u : __ldcg(a.alo + v);
+    const uint32_t top = e >= 31u ? e - 31u : 0u;
+    if (al != kFull && al != 0 && l0 <= e) open_window(a, q, r, v, e, max(l0, top), e, 1, al);
+    else open_window(a, q, r, v, e, coarse ? 0u : top, e, 0, d);
+}
+
+// Largest h in [fl, e] with ge(h) >= h, where ge(h) counts values >= h (non-
+// increasing in h); kFull when ge(fl) < fl.  Probes e, e-1, e-3, e-7, ...
+// (late drops are small), then bisects the last step.
+template <class Ge>
+__device__ __forceinline__ uint32_t gallop_hindex(Ge ge, uint32_t fl, uint32_t e) {
+    uint32_t bad = e + 1, t = 1, lo;
+    for (;;) {
+        const uint32_t cand = e - fl >= t - 1 ? e - (t - 1) : fl;
+        if (ge(cand) >= cand) { lo = cand; break; }
+        bad = cand;
+        if (cand == fl) return kFull;
+        t <<= 1;
     }
-    uint32_t c = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) c += (lane + 32u * k < d && x[k] >= lo) ? 1u : 0u;
-    *count = __reduce_add_sync(kFull, c);
+    uint32_t hi = bad - 1;   // ge(bad) < bad
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (ge(mid) >= mid) lo = mid; else hi = mid - 1;
+    }
     return lo;
 }
 
-// Phase A for the warp frontier (vertices of at most kHxWarpArcs arcs), 32
-// list entries per warp step.  The neighbours' estimates of as many whole
-// vertices as fit kBatchVals values are gathered into shared memory with all
+// Largest h in [fl, e] with at least h of the d values xs[0..d) >= h (d <=
+// kBatchVals, in shared memory), and the count at that h; kFull when fewer
+// than fl values are >= fl (the h-index lies below the floor).  One warp.
+__device__ __forceinline__ uint32_t warp_hindex(const uint32_t* xs, uint32_t d, uint32_t fl, uint32_t e,
+                                                uint32_t* count) {
+    const unsigned lane = lane_id();
+    constexpr int kPer = kBatchVals / 32;
+    uint32_t x[kPer];
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+        const uint32_t idx = lane + 32u * j;
+        x[j] = idx < d ? xs[idx] : 0u;
+    }
+    auto ge = [&](uint32_t h) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) c += (lane + 32u * j < d && x[j] >= h) ? 1u : 0u;
+        return __reduce_add_sync(kFull, c);
+    };
+    const uint32_t h = gallop_hindex(ge, fl, e);   // warp-uniform
+    if (h != kFull) *count = ge(h);
+    return h;
+}
+
+// Phase A for the warp frontier, 32 list entries per warp step: vertices of
+// at most kHxWarpArcs arcs (their adjacency) and large vertices whose active
+// list holds at most kBatchVals entries (entry flag kListFlag; the search
+// starts at the list's floor).  The neighbours' estimates of as many whole
+// entries as fit kBatchVals values are gathered into shared memory with all
 // loads in flight (the dependent load chain is paid once per batch, not once
-// per vertex); then the warp finds each vertex's h-index from shared memory.
-__device__ void warp_batch(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p, const uint32_t* list, uint32_t n,
-                           uint32_t wr, uint32_t nw) {
+// per vertex); then a lane (all degrees <= 32) or the warp finds each
+// h-index from shared memory.  An h-index below a list's floor sends the
+// vertex to a window search over its adjacency in the next pass.
+__device__ void warp_batch(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p, uint32_t r, const uint32_t* list,
+                           uint32_t n, uint32_t wr, uint32_t nw) {
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     uint32_t* vals = sh.vals[wid];
     uint32_t* pref = sh.wbin[wid];   // 33 words: exclusive prefix of the degrees + total
-    uint32_t* vs = sh.tstart[wid];
-    uint32_t* es = sh.told[wid];
     uint32_t* ss = sh.tnew[wid];
     // entries per warp step: enough for every warp to get a share, at most 32
     const uint32_t B = min(32u, max(1u, (n + nw - 1) / nw));
     for (uint32_t i0 = wr * B; i0 < n; i0 += nw * B) {
         const uint32_t i = i0 + lane;
-        uint32_t v = kFull, s0 = 0, d = 0, e = 0;
+        uint32_t v = kFull, s0 = 0, d = 0, e = 0, fl = 0, dfull = 0;
+        bool listed = false, below = false;
         if (lane < B && i < n) {
-            v = __ldcg(list + i);
+            const uint32_t ent = __ldcg(list + i);
+            v = ent & ~kListFlag;
+            listed = (ent & kListFlag) != 0;
             if (v < a.V) {
                 s0 = KC_LDG(a.off + v);
-                d = min(KC_LDG(a.off + v + 1) - s0, kHxWarpArcs);
+                dfull = KC_LDG(a.off + v + 1) - s0;
                 e = __ldcg(a.est + v);
+                if (listed) {
+                    const uint32_t al = __ldcg(a.alen + v);
+                    fl = __ldcg(a.alo + v);
+                    if (al == kFull || al > kBatchVals || al > dfull || fl > e) below = true;   // (cannot happen)
+                    else d = al;
+                } else {
+                    d = min(dfull, kHxWarpArcs);
+                }
             } else {
                 v = kFull;
             }
         }
+        const unsigned listm = __ballot_sync(kFull, listed);
         uint32_t total;
         const uint32_t ex = warp_excl_scan(d, &total);
         __syncwarp();
-        vs[lane] = v;
-        es[lane] = e;
         ss[lane] = s0;
         pref[lane] = ex;
         if (lane == 0) pref[32] = total;
         __syncwarp();
         uint32_t k0 = 0;
         while (k0 < 32) {   // warp-uniform
-            // the batch: vertices k0..k1-1, the most whose arcs fit kBatchVals
-            // (at least one: a degree is at most kHxWarpArcs <= kBatchVals)
+            // the batch: entries k0..k1-1, the most whose values fit kBatchVals
+            // (at least one: an entry holds at most kBatchVals)
             const uint32_t base = pref[k0];
             const unsigned fit = __ballot_sync(kFull, lane >= k0 && pref[lane + 1] - base <= kBatchVals);
             const uint32_t k1 = k0 + max(1u, (uint32_t)__popc(fit));
@@ -276,7 +352,8 @@ __device__ void warp_batch(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p
                             const uint32_t mid = (lo + hi) >> 1;
                             if (pref[mid] <= qa) lo = mid; else hi = mid;
                         }
-                        u[j] = KC_LDG(a.nbr + ss[lo] + (qa - pref[lo]));
+                        const uint32_t at = ss[lo] + (qa - pref[lo]);
+                        u[j] = (listm >> lo) & 1u ? __ldcg(a.act + at) : KC_LDG(a.nbr + at);
                     }
                 }
 #pragma unroll
@@ -286,41 +363,179 @@ __device__ void warp_batch(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p
                 }
             }
             __syncwarp();
-            for (uint32_t k = k0; k < k1; ++k) {   // warp-uniform
-                const uint32_t vk = vs[k];
+            const bool mine = lane >= k0 && lane < k1 && v != kFull;
+            uint32_t h = kFull, c = 0;
+            // entries of at most 32 values: a lane each, from shared memory
+            if (mine && !below && d <= 32) {
+                const uint32_t* xs = vals + (ex - base);
+                auto ge = [&](uint32_t t) {
+                    uint32_t k = 0;
+                    for (uint32_t i2 = 0; i2 < d; ++i2) k += xs[i2] >= t ? 1u : 0u;
+                    return k;
+                };
+                h = gallop_hindex(ge, fl, e);
+                if (h != kFull) c = ge(h);
+            }
+            // larger entries: the warp, one after another
+            unsigned big = __ballot_sync(kFull, mine && !below && d > 32);
+            while (big) {
+                const uint32_t k = __ffs(big) - 1;
+                big &= big - 1;
                 const uint32_t dk = pref[k + 1] - pref[k];
-                if (vk == kFull) continue;
-                const uint32_t ek = es[k], ok = pref[k] - base;
-                uint32_t x[8];
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const uint32_t idx = lane + 32u * j;
-                    x[j] = idx < dk ? vals[ok + idx] : 0u;
-                }
-                uint32_t c;
-                const uint32_t h = warp_hindex(x, dk, ek, &c);
-                if (lane == 0) {
-                    a.cnt[vk] = c;
-                    if (h < ek) {
-                        a.old[vk] = ek;
-                        a.est[vk] = h;
+                const uint32_t ek = __shfl_sync(kFull, e, k), fk = __shfl_sync(kFull, fl, k);
+                uint32_t ck = 0;
+                const uint32_t hk = warp_hindex(vals + (pref[k] - base), dk, fk, ek, &ck);
+                if (lane == k) { h = hk; c = ck; }
+            }
+            // results: the lane of each entry writes it
+            bool drop = false, two = false;
+            if (mine) {
+                if (below || h == kFull) {
+                    // h-index below the list's floor: search the adjacency, the
+                    // 32 values under the floor first
+                    if (dfull <= kHxCtaVals) {
+                        push_cta(a, r, v);   // the adjacency, read whole by a CTA next pass
+                    } else {
+                        const uint32_t hi = below ? e : fl - 1;
+                        open_window(a, p, r, v, e, hi >= 31u ? hi - 31u : 0u, hi, 0, dfull);
+                    }
+                } else {
+                    a.cnt[v] = c;
+                    if (h < e) {
+                        a.old[v] = e;
+                        a.est[v] = h;
+                        drop = true;
+                        two = listed && d > kHxChunk;
                     }
                 }
-                stage_bt(a, sh, st, p, h < ek ? 1u : 0u, (unsigned long long)vk << 32);
             }
+            const unsigned long long t0 = ((unsigned long long)v << 32) | (listed ? kListTask : 0u);
+            stage_bt(a, sh, st, p, __ballot_sync(kFull, drop), t0);
+            stage_bt(a, sh, st, p, __ballot_sync(kFull, two), t0 | 1u);
             __syncwarp();
             k0 = k1;
         }
     }
 }
 
+// CTA-wide sum of one value per thread (every thread gets it).
+__device__ __forceinline__ uint32_t cta_sum(uint32_t x, HxShared& sh) {
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    x = __reduce_add_sync(kFull, x);
+    __syncthreads();   // earlier readers of red[] are done
+    if (lane == 0) sh.red[wid] = x;
+    __syncthreads();
+    return __reduce_add_sync(kFull, lane < kWarps ? sh.red[lane] : 0u);
+}
+
+// Phase A for a large vertex read whole by one CTA (at most kHxCtaVals
+// entries): its active list (from the list's floor) or its adjacency (from 0,
+// rebuilding the list), gathered into shared memory; the h-index is exact in
+// one pass, with CTA reductions.  An h-index below the list's floor sends the
+// CTA on to the adjacency, or, above kHxCtaVals arcs, to a window search in
+// the next pass.
+__device__ void cta_entry(const HxArgs& a, HxShared& sh, uint32_t p, uint32_t r, uint32_t ent) {
+    const unsigned tid = threadIdx.x, lane = lane_id();
+    const uint32_t v = ent & ~kListFlag;
+    if (v >= a.V) return;
+    const uint32_t s0 = KC_LDG(a.off + v);
+    const uint32_t d = KC_LDG(a.off + v + 1) - s0;
+    const uint32_t e = __ldcg(a.est + v);
+    const uint32_t al = __ldcg(a.alen + v), fl0 = __ldcg(a.alo + v);
+    bool list = (ent & kListFlag) != 0 && al != kFull && al != 0 && al <= kHxCtaVals && al <= d && fl0 <= e;
+    uint32_t* vals = &sh.vals[0][0];
+    constexpr int kPer = kHxCtaVals / kPeelThreads;
+    for (int round = 0; round < 2; ++round) {   // the list, then (below its floor) the adjacency
+        const uint32_t len = list ? al : d;
+        const uint32_t fl = list ? fl0 : 0u;
+        if (len > kHxCtaVals) {   // (adjacency only) a window search in the next pass
+            if (tid == 0) {
+                const uint32_t hi = round == 0 ? e : fl0 - 1;
+                open_window(a, p, r, v, e, hi >= 31u ? hi - 31u : 0u, hi, 0, d);
+            }
+            break;
+        }
+        for (uint32_t i = tid; i < len; i += kPeelThreads) {
+            const uint32_t u = list ? __ldcg(a.act + s0 + i) : KC_LDG(a.nbr + s0 + i);
+            vals[i] = u < a.V ? __ldcg(a.est + u) : 0u;
+        }
+        __syncthreads();
+        uint32_t x[kPer];
+#pragma unroll
+        for (int j = 0; j < kPer; ++j) {
+            const uint32_t idx = tid + kPeelThreads * j;
+            x[j] = idx < len ? vals[idx] : 0u;
+        }
+        auto ge = [&](uint32_t h) {
+            uint32_t c = 0;
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) c += (tid + kPeelThreads * j < len && x[j] >= h) ? 1u : 0u;
+            return cta_sum(c, sh);
+        };
+        const uint32_t h = gallop_hindex(ge, fl, e);   // CTA-uniform
+        if (h == kFull) {   // below the list's floor
+            list = false;
+            __syncthreads();
+            continue;
+        }
+        const uint32_t c = ge(h);
+        uint32_t L = al;
+        if (!list) {
+            // rebuild the active list: the neighbours at or above h - kListMargin
+            const uint32_t nf = h > kListMargin ? h - kListMargin : 0u;
+            if (tid == 0) sh.cpos = 0;
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < kPer; ++j) {
+                const uint32_t idx = tid + kPeelThreads * j;
+                const bool keep = idx < len && x[j] >= nf;
+                const unsigned m = __ballot_sync(kFull, keep);
+                if (!m) continue;
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(&sh.cpos, (uint32_t)__popc(m));
+                base = __shfl_sync(kFull, base, 0);
+                if (keep) a.act[s0 + base + __popc(m & lanemask_lt())] = KC_LDG(a.nbr + s0 + idx);
+            }
+            __syncthreads();
+            L = sh.cpos;
+            if (tid == 0) {
+                a.alen[v] = L;
+                a.alo[v] = nf;
+            }
+        }
+        if (tid == 0) {
+            a.cnt[v] = c;
+            if (h < e) {
+                a.old[v] = e;
+                a.est[v] = h;
+            }
+        }
+        if (h < e && tid < 32) {   // update tasks over the active list
+            const uint32_t n = (L + kHxChunk - 1) / kHxChunk;
+            uint32_t base = 0;
+            if (lane == 0 && n) base = atomicAdd(&a.ctl->hx.bt_n[p], n);
+            base = __shfl_sync(kFull, base, 0);
+            for (uint32_t cc = lane; cc < n; cc += 32) {
+                if (base + cc < a.cap_bt) a.bt[p][base + cc] = ((unsigned long long)v << 32) | kListTask | cc;
+                else record_error(a.ctl, kErrOverflow, 0);
+            }
+        }
+        break;
+    }
+    __syncthreads();   // shared values reused by the next entry
+}
+
 // The warp that finished the last chunk of slot `s` reads the pass's bins.
+// Found (bins one wide): the h-index and its count; a drop queues update tasks
+// over the active list.  Otherwise the next pass narrows the window to the bin
+// that holds h, or, when h lies below the window, reads the range below it
+// (the whole adjacency once h is below the active list's floor).
 __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p, uint32_t r, uint32_t s) {
     const unsigned lane = lane_id();
     HxSlot* sl = a.slots[p] + s;
     uint32_t* bins = a.bins[p] + (size_t)s * kHxBinWords;
     const uint32_t v = __ldcg(&sl->v), e = __ldcg(&sl->e), lo = __ldcg(&sl->lo), hi = __ldcg(&sl->hi);
-    const uint32_t shft = __ldcg(&sl->sh), nch = __ldcg(&sl->nch);
+    const uint32_t shft = __ldcg(&sl->sh), mode = __ldcg(&sl->mode);
     const uint32_t nb = ((hi - lo) >> shft) + 1;
     __threadfence();
     const uint32_t cb = lane < nb ? __ldcg(bins + lane) : 0u;
@@ -338,13 +553,16 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
     const uint32_t S = suf + above;
     const uint32_t start = lo + (lane << shft);
     const unsigned ok = __ballot_sync(kFull, lane < nb && S >= start);
-    uint32_t nlo, nhi;
+    uint32_t nlo, nhi, nmode = mode;
     if (ok) {
         const uint32_t bs = 31 - __clz(ok);
         const uint32_t Sb = __shfl_sync(kFull, S, bs);
         const uint32_t sb = lo + (bs << shft);
         if (shft == 0) {   // found: h = sb, counted Sb
+            // a pass over the adjacency leaves the list of neighbours >= lo
+            const uint32_t L = mode == 0 ? __ldcg(a.alen + v) : __ldcg(&sl->len);
             if (lane == 0) {
+                if (mode == 0) a.alo[v] = lo > kListMargin ? lo - kListMargin : 0u;
                 a.cnt[v] = Sb;
                 if (sb < e) {
                     a.old[v] = e;
@@ -352,13 +570,15 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
                 }
             }
             if (sb < e) {
-                // update tasks for every chunk of v
+                // update tasks over the active list: a neighbour whose count
+                // this drop crosses has an estimate above sb >= alo[v]
+                const uint32_t n = (L + kHxChunk - 1) / kHxChunk;
                 HxCtl* hx = &a.ctl->hx;
                 uint32_t base = 0;
-                if (lane == 0) base = atomicAdd(&hx->bt_n[p], nch);
+                if (lane == 0 && n) base = atomicAdd(&hx->bt_n[p], n);
                 base = __shfl_sync(kFull, base, 0);
-                for (uint32_t c = lane; c < nch; c += 32) {
-                    if (base + c < a.cap_bt) a.bt[p][base + c] = ((unsigned long long)v << 32) | c;
+                for (uint32_t c = lane; c < n; c += 32) {
+                    if (base + c < a.cap_bt) a.bt[p][base + c] = ((unsigned long long)v << 32) | kListTask | c;
                     else record_error(a.ctl, kErrOverflow, 0);
                 }
             }
@@ -367,28 +587,39 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
         nlo = sb;
         nhi = min(sb + (1u << shft) - 1u, hi);
     } else {   // h < lo (lo > 0 here: at lo = 0 bin 0 always qualifies)
-        nlo = 0;
+        // the list still holds every neighbour down to its floor; below that
+        // the adjacency is read
+        const uint32_t fl = mode == 1 ? __ldcg(a.alo + v) : 0u;
         nhi = lo - 1;
+        if (mode == 1 && fl < lo) {
+            nlo = fl;
+        } else {
+            // the adjacency: once the 32 values under a top window or under
+            // the list's floor, then everything below
+            nlo = ((mode == 1 || hi == e) && nhi >= 31u) ? nhi - 31u : 0u;
+            nmode = 0;
+        }
     }
+    uint32_t len = __ldcg(&sl->len);
+    if (nmode == 0 && mode == 1) len = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
+    const uint32_t nch = (len + kHxChunk - 1) / kHxChunk;
     if (lane == 0) {
         sl->lo = nlo;
         sl->hi = nhi;
         sl->sh = bin_shift(nlo, nhi);
+        sl->mode = nmode;
+        sl->len = len;
+        sl->nch = nch;
         sl->done = 0;
+        if (nmode == 0) a.alen[v] = 0;   // the next pass rebuilds the list
         atomicAdd(&a.ctl->hx.passes, 1u);
     }
-    HxCtl* hx = &a.ctl->hx;
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(&hx->cl_n[(r + 1) % 3], nch);
-    base = __shfl_sync(kFull, base, 0);
-    if (base + nch > a.cap_cl) {
-        if (lane == 0) record_error(a.ctl, kErrOverflow, 0);
-        return;
-    }
-    for (uint32_t c = lane; c < nch; c += 32) a.cl[(r + 1) % 3][base + c] = ((unsigned long long)s << 32) | c;
+    queue_chunks(a, r, s, nch, lane, 32);
 }
 
-// Phase A for one chunk task of a large vertex: bin its neighbours' estimates.
+// Phase A for one chunk task of a large vertex: bin its neighbours' estimates
+// (of the adjacency or of the active list).  A pass over the adjacency also
+// appends every neighbour at or above the window's floor to the active list.
 __device__ void chunk_task(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p, uint32_t r,
                            unsigned long long task, bool degrees) {
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -396,22 +627,52 @@ __device__ void chunk_task(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p
     if (s >= a.cap_l) return;
     HxSlot* sl = a.slots[p] + s;
     const uint32_t v = __ldcg(&sl->v), lo = __ldcg(&sl->lo), hi = __ldcg(&sl->hi), shft = __ldcg(&sl->sh);
-    const uint32_t nch = __ldcg(&sl->nch);
+    const uint32_t nch = __ldcg(&sl->nch), mode = __ldcg(&sl->mode), total = __ldcg(&sl->len);
     if (v >= a.V) return;
     const uint32_t s0 = KC_LDG(a.off + v);
     const uint32_t d = KC_LDG(a.off + v + 1) - s0;
     const uint32_t b0 = c * kHxChunk;
-    const uint32_t len = b0 < d ? min(kHxChunk, d - b0) : 0u;
-    uint32_t bin[8];
+    const uint32_t len = (b0 < total && total <= d) ? min(kHxChunk, total - b0) : 0u;
+    uint32_t bin[8], uu[8], xv[8];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
         const uint32_t i = lane + 32u * k;
+        uu[k] = kFull;
+        if (i < len) uu[k] = mode ? __ldcg(a.act + s0 + b0 + i) : KC_LDG(a.nbr + s0 + b0 + i);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
         bin[k] = kNoBin;
-        if (i < len) {
-            const uint32_t u = KC_LDG(a.nbr + s0 + b0 + i);
-            uint32_t x = 0;
-            if (u < a.V) x = degrees ? KC_LDG(a.off + u + 1) - KC_LDG(a.off + u) : __ldcg(a.est + u);
+        xv[k] = 0;
+        if (uu[k] < a.V) {
+            const uint32_t u = uu[k];
+            const uint32_t x = degrees ? KC_LDG(a.off + u + 1) - KC_LDG(a.off + u) : __ldcg(a.est + u);
+            xv[k] = x;
             bin[k] = x > hi ? 32u : (x >= lo ? (x - lo) >> shft : kNoBin);
+        }
+    }
+    if (mode == 0) {   // rebuild the active list: the neighbours at or above lo - kListMargin
+        const uint32_t lfl = lo > kListMargin ? lo - kListMargin : 0u;
+        unsigned keep[8];
+        uint32_t nk = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            keep[k] = __ballot_sync(kFull, uu[k] < a.V && xv[k] >= lfl);
+            nk += __popc(keep[k]);
+        }
+        if (nk) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(a.alen + v, nk);
+            base = __shfl_sync(kFull, base, 0);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                if (keep[k] & (1u << lane)) {
+                    const uint32_t pos = base + __popc(keep[k] & lanemask_lt());
+                    if (pos < d) a.act[s0 + pos] = uu[k];
+                    else record_error(a.ctl, kErrOverflow, 0);
+                }
+                base += __popc(keep[k]);
+            }
         }
     }
     uint32_t* wb = sh.wbin[wid];
@@ -457,19 +718,23 @@ __device__ void update_tasks(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
         const uint64_t i64 = (m0 + lane) * nw + wr;
         const uint32_t i = (uint32_t)i64;
         uint32_t len = 0, s1 = 0, ol = 0, nw_ = 0;
+        bool listed = false;
         if (lane < T && i64 < nbt) {
             const unsigned long long tk = __ldcg(a.bt[p] + i);
-            const uint32_t u = (uint32_t)(tk >> 32), c = (uint32_t)tk;
+            const uint32_t u = (uint32_t)(tk >> 32), c = (uint32_t)tk & ~kListTask;
+            listed = ((uint32_t)tk & kListTask) != 0;
             if (u < a.V) {
                 const uint32_t s0 = KC_LDG(a.off + u);
                 const uint32_t d = KC_LDG(a.off + u + 1) - s0;
+                const uint32_t n = listed ? min(__ldcg(a.alen + u), d) : d;
                 const uint32_t b0 = c * kHxChunk;
-                len = b0 < d ? min(kHxChunk, d - b0) : 0u;
+                len = b0 < n ? min(kHxChunk, n - b0) : 0u;
                 s1 = s0 + b0;
                 ol = __ldcg(a.old + u);
                 nw_ = __ldcg(a.est + u);
             }
         }
+        const unsigned listm = __ballot_sync(kFull, listed);   // tasks that read an active list
         uint32_t total;
         const uint32_t ex = warp_excl_scan(len, &total);
         pref[lane] = ex;
@@ -479,13 +744,14 @@ __device__ void update_tasks(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
         tnew[lane] = nw_;
         __syncwarp();
         uint32_t lo = 0;
-        for (uint32_t q0 = 0; q0 < total; q0 += 128) {
-            uint32_t wv[4], xv[4], kk[4];
+        for (uint32_t q0 = 0; q0 < total; q0 += 256) {
+            // neighbour ids, then their estimates, then the decrements: each
+            // step's loads are all in flight before the next step uses them
+            uint32_t wv[8], kk[8];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < 8; ++j) {
                 const uint32_t qi = q0 + 32u * j + lane;
                 wv[j] = kFull;
-                xv[j] = 0;
                 kk[j] = 0;
                 if (qi < total) {
                     uint32_t hi = 32;
@@ -494,35 +760,42 @@ __device__ void update_tasks(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
                         if (pref[mid] <= qi) lo = mid; else hi = mid;
                     }
                     kk[j] = lo;
-                    const uint32_t w = KC_LDG(a.nbr + tstart[lo] + (qi - pref[lo]));
-                    if (w < a.V) {
-                        wv[j] = w;
-                        xv[j] = __ldcg(a.est + w);
-                    }
+                    const uint32_t at = tstart[lo] + (qi - pref[lo]);
+                    wv[j] = (listm >> lo) & 1u ? __ldcg(a.act + at) : KC_LDG(a.nbr + at);
                 }
             }
-            unsigned push_m = 0;
-            uint32_t push_v = kFull;
+            uint32_t xv[8];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                bool queue = false;
-                if (wv[j] != kFull) {
-                    const uint32_t x = xv[j];
-                    if (tnew[kk[j]] < x && x <= told[kk[j]]) {
-                        const uint32_t y = atomicSub(a.cnt + wv[j], 1u);
-                        queue = (y == x);
+            for (int j = 0; j < 8; ++j) xv[j] = wv[j] < a.V ? __ldcg(a.est + wv[j]) : 0u;
+            uint32_t y[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                y[j] = kFull;
+                if (wv[j] < a.V && tnew[kk[j]] < xv[j] && xv[j] <= told[kk[j]]) y[j] = atomicSub(a.cnt + wv[j], 1u);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                bool queue = y[j] != kFull && y[j] == xv[j];
+                // queue: small and mid-size vertices to the warp list, large ones to a slot
+                uint32_t ent = wv[j];
+                if (queue) {
+                    const uint32_t dq = KC_LDG(a.off + wv[j] + 1) - KC_LDG(a.off + wv[j]);
+                    if (dq > kHxWarpArcs) {
+                        // a short active list: the warp path; up to kHxCtaVals entries
+                        // (list or adjacency): the CTA path; else a window slot
+                        const uint32_t al = __ldcg(a.alen + wv[j]);
+                        const bool usable = al != kFull && al != 0 && __ldcg(a.alo + wv[j]) <= xv[j];
+                        if (usable && al <= kBatchVals) {
+                            ent |= kListFlag;
+                        } else {
+                            if (usable && al <= kHxCtaVals) push_cta(a, r, wv[j] | kListFlag);
+                            else if (!usable && dq <= kHxCtaVals) push_cta(a, r, wv[j]);
+                            else open_slot(a, q, r, wv[j], xv[j], dq, false);
+                            queue = false;
+                        }
                     }
                 }
-                // queue: small and mid-size vertices to the warp list, large ones to a slot
-                uint32_t dq = 0;
-                if (queue) dq = KC_LDG(a.off + wv[j] + 1) - KC_LDG(a.off + wv[j]);
-                if (queue && dq > kHxWarpArcs) {
-                    open_slot(a, q, r, wv[j], xv[j], dq, false);
-                    queue = false;
-                }
-                push_m = __ballot_sync(kFull, queue);
-                push_v = wv[j];
-                stage_rm(a, sh, st, q, push_m, push_v);
+                stage_rm(a, sh, st, q, __ballot_sync(kFull, queue), ent);
             }
         }
         __syncwarp();
@@ -541,57 +814,78 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
     const uint32_t wr = wid * gridDim.x + blockIdx.x;
     const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
     if (a.max_level == kFull && ld_err(&ctl->err)) return;   // the device validation refused the CSR
+    if (threadIdx.x == 0) sh.bar_k = 0;
     Stager st;
 
-    // Sub-phase 0: est = degree.
-    for (uint32_t v = gw * 32 + lane; v < a.V; v += nw * 32) a.est[v] = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
+    // Sub-phase 0: est = degree, no active lists.
+    for (uint32_t v = gw * 32 + lane; v < a.V; v += nw * 32) {
+        a.est[v] = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
+        a.alen[v] = kFull;
+    }
     if (!hx_barrier(a, sh)) return;
 
     // Iteration 1, first sweep (sub-phase 1): a lane per vertex of at most
-    // kHxLaneArcs arcs; larger vertices are queued for phase A (parity 1).
+    // kHxLaneArcs arcs, two such vertices in flight per lane (blocks of 64
+    // consecutive vertices per warp); larger vertices are queued for phase A
+    // (parity 1).
     uint32_t r = 1;
     {
-        for (uint32_t base = gw * 32; base < a.V; base += nw * 32) {
-            const uint32_t v = base + lane;
-            uint32_t s0 = 0, d = 0;
-            if (v < a.V) {
-                s0 = KC_LDG(a.off + v);
-                d = KC_LDG(a.off + v + 1) - s0;
-            }
-            const bool small = v < a.V && d <= kHxLaneArcs;
-            bool drop = false;
-            if (small) {
-                uint32_t x[kHxLaneArcs];
+        for (uint32_t base = gw * 64; base < a.V; base += nw * 64) {
+            uint32_t vv[2], s0[2], d[2];
 #pragma unroll
-                for (uint32_t i = 0; i < kHxLaneArcs; ++i) {
-                    x[i] = 0;
-                    if (i < d) {
-                        const uint32_t u = KC_LDG(a.nbr + s0 + i);
-                        x[i] = u < a.V ? __ldcg(a.est + u) : 0u;
-                    }
+            for (int h = 0; h < 2; ++h) {
+                vv[h] = base + 32u * h + lane;
+                s0[h] = 0;
+                d[h] = 0;
+                if (vv[h] < a.V) {
+                    s0[h] = KC_LDG(a.off + vv[h]);
+                    d[h] = KC_LDG(a.off + vv[h] + 1) - s0[h];
                 }
-                uint32_t lo = 0, hi = d;
-                while (lo < hi) {
-                    const uint32_t mid = (lo + hi + 1) >> 1;
+            }
+            uint32_t x[2][kHxLaneArcs];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t dl = (vv[h] < a.V && d[h] <= kHxLaneArcs) ? d[h] : 0u;
+#pragma unroll
+                for (uint32_t i = 0; i < kHxLaneArcs; ++i) x[h][i] = i < dl ? KC_LDG(a.nbr + s0[h] + i) : kFull;
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+#pragma unroll
+                for (uint32_t i = 0; i < kHxLaneArcs; ++i) x[h][i] = x[h][i] < a.V ? __ldcg(a.est + x[h][i]) : 0u;
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t v = vv[h], dv = d[h];
+                const bool small = v < a.V && dv <= kHxLaneArcs;
+                bool drop = false;
+                if (small) {
+                    uint32_t lo = 0, hi = dv;
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi + 1) >> 1;
+                        uint32_t c = 0;
+#pragma unroll
+                        for (uint32_t i = 0; i < kHxLaneArcs; ++i) c += (i < dv && x[h][i] >= mid) ? 1u : 0u;
+                        if (c >= mid) lo = mid; else hi = mid - 1;
+                    }
                     uint32_t c = 0;
 #pragma unroll
-                    for (uint32_t i = 0; i < kHxLaneArcs; ++i) c += (i < d && x[i] >= mid) ? 1u : 0u;
-                    if (c >= mid) lo = mid; else hi = mid - 1;
+                    for (uint32_t i = 0; i < kHxLaneArcs; ++i) c += (i < dv && x[h][i] >= lo) ? 1u : 0u;
+                    a.cnt[v] = c;
+                    if (lo < dv) {
+                        a.old[v] = dv;
+                        a.est[v] = lo;
+                        drop = true;
+                    }
                 }
-                uint32_t c = 0;
-#pragma unroll
-                for (uint32_t i = 0; i < kHxLaneArcs; ++i) c += (i < d && x[i] >= lo) ? 1u : 0u;
-                a.cnt[v] = c;
-                if (lo < d) {
-                    a.old[v] = d;
-                    a.est[v] = lo;
-                    drop = true;
+                stage_bt(a, sh, st, 1, __ballot_sync(kFull, drop), (unsigned long long)v << 32);
+                const bool mid = v < a.V && dv > kHxLaneArcs && dv <= kHxWarpArcs;
+                stage_rm(a, sh, st, 1, __ballot_sync(kFull, mid), v);
+                if (v < a.V && dv > kHxWarpArcs) {
+                    if (dv <= kHxCtaVals) push_cta(a, 0, v);
+                    else open_slot(a, 1, 0, v, dv, dv, true);
                 }
             }
-            stage_bt(a, sh, st, 1, __ballot_sync(kFull, drop), (unsigned long long)v << 32);
-            const bool mid = v < a.V && d > kHxLaneArcs && d <= kHxWarpArcs;
-            stage_rm(a, sh, st, 1, __ballot_sync(kFull, mid), v);
-            if (v < a.V && d > kHxWarpArcs) open_slot(a, 1, 0, v, d, d, true);
         }
         flush_bt(a, sh, st, 1);
         flush_rm(a, sh, st, 1);
@@ -606,10 +900,15 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
         bool first = true;
         for (;;) {
             const uint32_t ncl = min(ld_relaxed(&hx->cl_n[r % 3]), a.cap_cl);
+            const uint32_t nrc = min(ld_relaxed(&hx->rc_n[r % 3]), a.cap_l);
             const uint32_t nrm = first ? min(ld_relaxed(&hx->rm_n[p]), a.V) : 0u;
-            if (ncl == 0 && nrm == 0) break;   // every CTA reads the same counts
-            if (lead) hx->cl_n[(r + 2) % 3] = 0;
-            if (nrm) warp_batch(a, sh, st, p, a.rm[p], nrm, wr, nw);
+            if (ncl == 0 && nrm == 0 && nrc == 0) break;   // every CTA reads the same counts
+            if (lead) {
+                hx->cl_n[(r + 2) % 3] = 0;
+                hx->rc_n[(r + 2) % 3] = 0;
+            }
+            for (uint32_t i = blockIdx.x; i < nrc; i += gridDim.x) cta_entry(a, sh, p, r, __ldcg(a.rc[r % 3] + i));
+            if (nrm) warp_batch(a, sh, st, p, r, a.rm[p], nrm, wr, nw);
             for (uint32_t i = wr; i < ncl; i += nw) chunk_task(a, sh, st, p, r, __ldcg(a.cl[r % 3] + i), t == 1);
             flush_bt(a, sh, st, p);
             if (!hx_barrier(a, sh)) return;
@@ -619,6 +918,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
         // ---- phase B (sub-phase r)
         if (lead) {
             hx->cl_n[(r + 2) % 3] = 0;
+            hx->rc_n[(r + 2) % 3] = 0;
             hx->bt_n[p ^ 1u] = 0;
             hx->rm_n[p] = 0;
             hx->rl_n[p] = 0;
@@ -628,7 +928,8 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
         if (!hx_barrier(a, sh)) return;
         ++r;
         const uint32_t nm = ld_relaxed(&hx->rm_n[p ^ 1u]), nl = ld_relaxed(&hx->rl_n[p ^ 1u]);
-        if (nm == 0 && nl == 0) break;
+        const uint32_t nc = ld_relaxed(&hx->rc_n[r % 3]);
+        if (nm == 0 && nl == 0 && nc == 0) break;
         ++t;
         if (t > a.max_iters) {   // the level peel takes over
             if (lead) hx->iters = t;
