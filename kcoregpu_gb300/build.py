@@ -33,7 +33,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr
                      "-Xcompiler", "-fPIC,-fopenmp,-O3,-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}", f"-I{CSRC}"]
 
-CU_SOURCES = ["kc_peel.cu", "kc_tail.cu", "kc_hindex.cu", "kc_validate.cu", "kc_api.cu", "kc_noalloc.cu", "kc_batch.cu", "kc_batch_host.cu",
+CU_SOURCES = ["kc_peel.cu", "kc_tail.cu", "kc_hindex.cu", "kc_hxtail.cu", "kc_validate.cu", "kc_api.cu", "kc_noalloc.cu", "kc_batch.cu", "kc_batch_host.cu",
               "kc_serve.cu"]
 CXX_SOURCES = ["kc_host.cpp", "kc_gen.cpp"]
 CHECKED_SOURCES = ["kc_peel.cu"]

@@ -221,14 +221,16 @@ const Overrides& overrides() {
     return o;
 }
 
-// Method of the single-graph peel when a graph asks for none: the level peel,
-// or the h-index fixed point (kc_hindex.cu) with the level peel as its
-// fallback when KC_ALGO=hindex (read once per process).
+// Method of the single-graph peel when a graph asks for none: the h-index
+// fixed point (kc_hindex.cu) with the level peel as its fallback, or, with
+// KC_ALGO=peel (read once per process), the level peel.  On GB300 the h-index
+// peel measured 1.94 / 2.09 / 2.01 ms on R-MAT 400K / 2^20 / Chung-Lu 2.4M
+// against 1.99 / 2.27 / 2.33 ms for the level peel.
 bool hindex_default() {
-    static bool on = false;
+    static bool on = true;
     static std::once_flag once;
     std::call_once(once, [] {
-        if (const char* e = std::getenv("KC_ALGO")) on = std::strcmp(e, "hindex") == 0;
+        if (const char* e = std::getenv("KC_ALGO")) on = std::strcmp(e, "peel") != 0;
     });
     return on;
 }
@@ -379,6 +381,61 @@ int reserve_hx(kc_graph* g) {
     g->hx_cap_cl = (uint32_t)cap_cl;
     g->hx_cap_bt = (uint32_t)cap_bt;
     return KC_OK;
+}
+
+// The cluster h-index tail (kc_hxtail.cu) on device `dev`: its shared-memory
+// and 16-CTA cluster opt-ins set, or null where such a cluster cannot run or
+// was not asked for: KC_TAIL=hindex (read once per process) sends the tails
+// to it; by default every tail goes to the level tail, which measured faster
+// on the benchmark graphs.
+const void* hxtail_kernel(int dev) {
+    static std::mutex mu;
+    static std::vector<int> state;   // 0 unknown, 1 usable, 2 not
+    static const bool off = [] {
+        const char* e = std::getenv("KC_TAIL");
+        return !(e && std::strcmp(e, "hindex") == 0);
+    }();
+    if (off) return nullptr;
+    std::lock_guard<std::mutex> lk(mu);
+    if ((int)state.size() <= dev) state.resize(dev + 1, 0);
+    if (state[dev] == 0) {
+        const void* fn = peel_hxtail_fn();
+        bool ok = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)peel_hxtail_smem()) ==
+                      cudaSuccess &&
+                  cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess;
+        if (ok) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(peel_hxtail_cluster());
+            cfg.blockDim = dim3(peel_hxtail_threads());
+            cfg.dynamicSmemBytes = peel_hxtail_smem();
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = peel_hxtail_cluster();
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int nc = 0;
+            ok = cudaOccupancyMaxActiveClusters(&nc, fn, &cfg) == cudaSuccess && nc >= 1;
+        }
+        cudaGetLastError();   // (a refused opt-in is not an error of the next call)
+        state[dev] = ok ? 1 : 2;
+    }
+    return state[dev] == 1 ? peel_hxtail_fn() : nullptr;
+}
+
+// Iterations after which the cluster h-index tail leaves the survivors to the
+// level tail (KC_HX_TAIL_ITERS, default 512).
+uint32_t hxtail_max_iters() {
+    static uint32_t n = 512;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (const char* e = std::getenv("KC_HX_TAIL_ITERS")) {
+            const long long x = std::atoll(e);
+            if (x >= 1 && x <= (1 << 24)) n = (uint32_t)x;
+        }
+    });
+    return n;
 }
 
 // The tail kernel with its shared-memory opt-in set on device `dev`.
@@ -609,8 +666,28 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         void* hargs[] = {&h};
         KC_CUDA(cudaLaunchCooperativeKernel(peel_hindex_fn(), dim3(g->grid), dim3(kPeelThreads), hargs, 0, g->stream));
     }
+    // The survivors handed over go to the cluster h-index tail first (not for
+    // the peel order or the per-level trace, which follow the level tail);
+    // the level tail kernel returns at once when it finished them.
+    const void* hxt = (tail && !with_order && !with_trace) ? hxtail_kernel(g->dev) : nullptr;
+    a.tail_hx_iters = hxt ? hxtail_max_iters() : 0u;
     void* args[] = {&a};
     KC_CUDA(cudaLaunchCooperativeKernel(peel_kernel(), dim3(g->grid), dim3(kPeelThreads), args, 0, g->stream));
+    if (hxt) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(peel_hxtail_cluster());
+        cfg.blockDim = dim3(peel_hxtail_threads());
+        cfg.dynamicSmemBytes = peel_hxtail_smem();
+        cfg.stream = g->stream;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = peel_hxtail_cluster();
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        KC_CUDA(cudaLaunchKernelExC(&cfg, hxt, args));
+    }
     if (tail)
         KC_CUDA(cudaLaunchKernel(tail_kernel(g->dev), dim3(1), dim3(kTailThreads), args, peel_tail_smem(), g->stream));
     KC_CUDA(cudaEventRecord(g->ev1, g->stream));

@@ -103,6 +103,9 @@ struct alignas(128) HxCtl {
     unsigned int pad5[31];
     unsigned int rc_n[3];      // CTA entries (large vertices read whole by one CTA), by sub-phase mod 3
     unsigned int pad6[29];
+    unsigned int tail_solved;  // 1: the cluster h-index tail found the survivors' core numbers
+    unsigned int tail_iters;   // its iterations
+    unsigned int pad7[30];
 };
 
 struct alignas(128) PeelCtl {
@@ -227,6 +230,8 @@ struct PeelArgs {
                                 // for kernels that peel many graphs at once)
     uint32_t hub_arcs = kLocalArcs;   // vertices with more arcs are queued as tasks instead of walked inline
     uint32_t chunk_arcs = kChunk;     // arcs per queued task, kMinChunk..kChunk
+    uint32_t tail_hx_iters = 0;       // > 0: the cluster h-index tail (kc_hxtail.cu) runs first, for at most
+                                      // this many iterations; the level tail kernel finishes otherwise
 };
 
 // Tail peel: one CTA of kTailThreads threads, states in shared memory.

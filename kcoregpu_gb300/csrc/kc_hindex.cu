@@ -61,7 +61,8 @@ constexpr uint32_t kWarps = kPeelThreads / 32;
 constexpr uint32_t kNoBin = 0xFFu;
 constexpr uint32_t kBatchVals = 512;   // neighbour estimates a warp gathers into shared memory at once
 constexpr uint32_t kListTask = 0x80000000u;   // update task flag: scan the active list, not the adjacency
-constexpr uint32_t kListMargin = 32;   // a rebuilt list also keeps neighbours this far below the window
+constexpr uint32_t kListMargin = 64;   // a rebuilt list also keeps neighbours this far below the window
+constexpr uint32_t kListGuard = 4;     // an estimate this close to its list's floor rebuilds the list first
 constexpr uint32_t kListFlag = 0x80000000u;   // warp-frontier entry flag: a large vertex read from its active list
 
 struct HxShared {
@@ -783,8 +784,10 @@ __device__ void update_tasks(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
                     if (dq > kHxWarpArcs) {
                         // a short active list: the warp path; up to kHxCtaVals entries
                         // (list or adjacency): the CTA path; else a window slot
+                        // (a list whose floor is within kListGuard of the estimate is
+                        // rebuilt now, before the h-index can fall below it)
                         const uint32_t al = __ldcg(a.alen + wv[j]);
-                        const bool usable = al != kFull && al != 0 && __ldcg(a.alo + wv[j]) <= xv[j];
+                        const bool usable = al != kFull && al != 0 && __ldcg(a.alo + wv[j]) + kListGuard <= xv[j];
                         if (usable && al <= kBatchVals) {
                             ent |= kListFlag;
                         } else {
@@ -881,10 +884,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
                 stage_bt(a, sh, st, 1, __ballot_sync(kFull, drop), (unsigned long long)v << 32);
                 const bool mid = v < a.V && dv > kHxLaneArcs && dv <= kHxWarpArcs;
                 stage_rm(a, sh, st, 1, __ballot_sync(kFull, mid), v);
-                if (v < a.V && dv > kHxWarpArcs) {
-                    if (dv <= kHxCtaVals) push_cta(a, 0, v);
-                    else open_slot(a, 1, 0, v, dv, dv, true);
-                }
+                if (v < a.V && dv > kHxWarpArcs) open_slot(a, 1, 0, v, dv, dv, true);
             }
         }
         flush_bt(a, sh, st, 1);
@@ -907,7 +907,19 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
                 hx->cl_n[(r + 2) % 3] = 0;
                 hx->rc_n[(r + 2) % 3] = 0;
             }
-            for (uint32_t i = blockIdx.x; i < nrc; i += gridDim.x) cta_entry(a, sh, p, r, __ldcg(a.rc[r % 3] + i));
+            if (nrc <= 2 * gridDim.x) {
+                for (uint32_t i = blockIdx.x; i < nrc; i += gridDim.x) cta_entry(a, sh, p, r, __ldcg(a.rc[r % 3] + i));
+            } else {
+                // too many for one CTA each: window searches spread over every
+                // warp, from the next pass
+                for (uint32_t i = gw * 32 + lane; i < nrc; i += nw * 32) {
+                    const uint32_t ent = __ldcg(a.rc[r % 3] + i), v = ent & ~kListFlag;
+                    if (v < a.V) {
+                        const uint32_t d = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
+                        open_slot(a, p, r, v, __ldcg(a.est + v), d, false);
+                    }
+                }
+            }
             if (nrm) warp_batch(a, sh, st, p, r, a.rm[p], nrm, wr, nw);
             for (uint32_t i = wr; i < ncl; i += nw) chunk_task(a, sh, st, p, r, __ldcg(a.cl[r % 3] + i), t == 1);
             flush_bt(a, sh, st, p);

@@ -19,6 +19,14 @@ uint32_t wait_limit_us();
 // shared memory), launched after the persistent kernel on the same stream.
 const void* peel_tail_fn();
 size_t peel_tail_smem();
+// Cluster h-index tail (kc_hxtail.cu): one cluster of peel_hxtail_cluster()
+// CTAs of peel_hxtail_threads() threads and peel_hxtail_smem() bytes of
+// dynamic shared memory, launched after the persistent kernel and before the
+// level tail kernel.
+const void* peel_hxtail_fn();
+size_t peel_hxtail_smem();
+int peel_hxtail_cluster();
+int peel_hxtail_threads();
 // h-index peel (kc_hindex.cu): one cooperative launch of kPeelThreads-thread
 // CTAs, one per SM, launched before the persistent kernel, which returns at
 // once when it set HxCtl::solved.

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kTailThreads, 1) peel_tail_kernel(const __grid
     PeelCtl* ctl = a.ctl;
     const unsigned tid = threadIdx.x, lane = tid & 31;
     const uint32_t n = ctl->tail_n;
-    if (n == 0 || ctl->err != 0) return;
+    if (n == 0 || ctl->err != 0 || ctl->hx.tail_solved) return;   // (the cluster h-index tail finished it)
     if (n > kTailV || n > a.tail_cap_v) {
         if (tid == 0) record_error(ctl, kErrOverflow, ctl->tail_level);
         return;

@@ -1,9 +1,9 @@
 """The h-index peel (kcoregpu_gb300/csrc/kc_hindex.cu) against the oracle.
 
-A graph set to the h-index method (kc_graph_set_method, or KC_ALGO=hindex as
-the process default) runs the h-index fixed point first when no peel order or
-trace is asked for; the level peel runs only when it gives up (KC_HX_ITERS
-iterations, default 256).  The core numbers must equal the oracle's bit for
+The h-index fixed point is the default method of a graph (kc_graph_set_method
+selects per graph, KC_ALGO=peel|hindex sets the process default): it runs
+first when no peel order or trace is asked for, and the level peel runs only
+when it gives up (KC_HX_ITERS iterations, default 256).  The core numbers must equal the oracle's bit for
 bit either way, and `stats["method"]` says which one produced them (1 =
 h-index).  Shapes: hubs far above the chunk size (windows narrowed over
 several passes), cliques and bipartite cores (every estimate falls together),
@@ -11,9 +11,9 @@ paths and cycles (one hop per iteration), isolated vertices, random R-MAT,
 Chung-Lu and Erdos-Renyi graphs, and raw CSRs with duplicate arcs and
 self-loops (compared with the reference's level-synchronous algorithm, which
 counts each arc).  Child processes pin the process default and the
-fallback: KC_ALGO=hindex sends the one-shot entry through the h-index,
-KC_HX_ITERS=2 stops it early and the level peel finishes, and a graph set to
-the level peel runs it alone.
+fallback: by default the one-shot entry goes through the h-index,
+KC_HX_ITERS=2 stops it early and the level peel finishes, KC_ALGO=peel makes
+the level peel the default, and a graph set to the level peel runs it alone.
 """
 import json
 import os
@@ -172,18 +172,18 @@ print(json.dumps(res))
 """
 
 
-def test_process_default_hindex_and_one_shot_entry(gpu):
-    out = _child(CHILD, KC_ALGO="hindex")
+def test_process_default_is_hindex_and_one_shot_entry(gpu):
+    out = _child(CHILD)
     assert out == {"chunglu": [[True, 1], [True, 0], True], "rmat": [[True, 1], [True, 0], True]}
 
 
 def test_early_stop_hands_over_to_the_level_peel(gpu):
-    out = _child(CHILD, KC_ALGO="hindex", KC_HX_ITERS=2)
+    out = _child(CHILD, KC_HX_ITERS=2)
     assert out == {"chunglu": [[True, 0], [True, 0], True], "rmat": [[True, 0], [True, 0], True]}
 
 
-def test_level_peel_is_the_default(gpu):
-    out = _child(CHILD)
+def test_level_peel_as_process_default(gpu):
+    out = _child(CHILD, KC_ALGO="peel")
     assert out == {"chunglu": [[True, 0], [True, 0], True], "rmat": [[True, 0], [True, 0], True]}
 
 

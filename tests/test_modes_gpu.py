@@ -3,7 +3,10 @@
 The level-peel settings are run with KC_ALGO=peel (the h-index peel, which
 runs first by default, would otherwise solve these graphs before the level
 peel starts); KC_ALGO=hindex runs the h-index peel, and KC_HX_ITERS=3 stops
-it early so that the level peel finishes from scratch.
+it early so that the level peel finishes from scratch.  With KC_TAIL=hindex
+the survivors handed to the tail go to the cluster h-index tail (16-CTA
+cluster, estimates in distributed shared memory); with KC_HX_TAIL_ITERS=2 it
+gives up and the level tail finishes them.
 The settings are read once per process (KC_CLAIM_CAS: claim by CAS or read
 the state first; KC_TAIL_V: the tail hand-off point, 0 = the persistent
 kernel peels every level; KC_LOCAL_BUDGET: the cascade budget, its minimum
@@ -65,7 +68,9 @@ LEVEL_PEEL = [
 
 
 @pytest.mark.parametrize("env", [{"KC_ALGO": "peel", **e} for e in LEVEL_PEEL] +
-                         [{"KC_ALGO": "hindex"}, {"KC_ALGO": "hindex", "KC_HX_ITERS": "3"}],
+                         [{"KC_ALGO": "hindex"}, {"KC_ALGO": "hindex", "KC_HX_ITERS": "3"},
+                          {"KC_ALGO": "peel", "KC_TAIL": "hindex"},
+                          {"KC_ALGO": "peel", "KC_TAIL": "hindex", "KC_HX_TAIL_ITERS": "2"}],
                          ids=lambda e: ",".join(f"{k}={v}" for k, v in e.items()))
 def test_peel_under_each_setting(gpu, env):
     r = subprocess.run([sys.executable, "-c", CHILD, str(ROOT)], env={**os.environ, **env},
