@@ -42,12 +42,14 @@ L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
 TIMING_NOTE = ("GPU arm: L2 flushed between timed steps (512 MiB write), inputs resident in HBM; "
                "reference arm: host memory")
 
-# DRAM bytes (read + write) of one peel -- the persistent kernel plus the
-# one-CTA tail kernel it hands the last levels to -- per workload, from one ncu
-# capture of that workload with the build that is measured here; None where
-# not captured.
-NCU_TRAFFIC = {1: 27_792_896 + 837_120 + 11_156_224, 2: 45_363_200 + 3_072_768 + 6_451_968 + 4_608,
-               3: 51_795_968 + 6_880_512 + 5_824_256}
+# DRAM bytes (read + write) of one peel per workload, from one ncu capture of
+# that workload with the build that is measured here: the h-index kernel plus
+# the level peel's persistent and tail kernels (which return at once after it),
+# and, for the level peel method, its persistent and one-CTA tail kernels.
+NCU_TRAFFIC = {1: 30_136_320 + 823_552 + 65_792 + 28_672, 2: 60_747_264 + 16_284_416 + 64_256 + 29_184,
+               3: 93_990_400 + 36_610_304 + 66_048 + 29_184}
+NCU_TRAFFIC_LEVEL_PEEL = {1: 27_792_896 + 837_120 + 11_156_224, 2: 45_363_200 + 3_072_768 + 6_451_968 + 4_608,
+                          3: 51_795_968 + 6_880_512 + 5_824_256}
 
 
 def dist_env():
@@ -321,7 +323,7 @@ def single_leg(cfg: int, args, torch, flush, local: int, world: int, steps: int,
     g.set_stream(stream.cuda_stream)
 
     # correctness of the benchmarked graph (untimed)
-    core, kmax, _ = g.peel()
+    core, kmax, st0 = g.peel()
     want, wk = O.bz(off, nbr)
     if not (np.array_equal(core, want) and kmax == wk):
         raise SystemExit(f"bench: GPU core numbers differ from the oracle on {W.SINGLE[cfg]['name']}")
@@ -365,8 +367,13 @@ def single_leg(cfg: int, args, torch, flush, local: int, world: int, steps: int,
            "hbm_gbs": achieved,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "peak_kind": peak_kind + " hbm_gbs",
-                        "algorithmic_bytes": B, "traffic": NCU_TRAFFIC.get(cfg)},
-           "gpu_launches": 2 * steps,   # persistent peel + tail kernel per step
+                        "algorithmic_bytes": B,
+                        "traffic": (NCU_TRAFFIC if st0["method"] == 1 else NCU_TRAFFIC_LEVEL_PEEL).get(cfg)},
+           "method": "hindex" if st0["method"] == 1 else "level peel", "iterations": st0["iterations"],
+           # per step: the h-index kernel (h-index method), the persistent peel
+           # kernel and the tail kernel (both return at once after an h-index
+           # peel that converged)
+           "gpu_launches": (3 if st0["method"] == 1 else 2) * steps,
            "clocks": clk.summary(), "wall_s": t_wall, "bit_exact_vs_oracle": True}
     if args.profile:
         g.free()
