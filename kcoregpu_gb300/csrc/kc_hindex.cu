@@ -806,6 +806,75 @@ __device__ void update_tasks(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
     flush_rm(a, sh, st, q);
 }
 
+// The CTAs of an iteration.  cta/ncta: this CTA's rank and the CTAs taking
+// part; gw: warp rank for linear sweeps; wr/nw: warp rank for work lists
+// (consecutive ranks on different SMs) and the warps taking part.
+struct Exec {
+    uint32_t cta, ncta, gw, wr, nw;
+    bool lead;
+};
+
+// One iteration (phase A passes, then phase B) from sub-phase r; t and r
+// advance.  Returns 0: another iteration has work, 1: converged, 2: the
+// iteration budget is spent, -1: a barrier failed (error recorded).
+__device__ int hx_iteration(const HxArgs& a, HxShared& sh, Stager& st, uint32_t& t, uint32_t& r, const Exec& ex) {
+    HxCtl* hx = &a.ctl->hx;
+    const unsigned lane = lane_id();
+    const uint32_t p = t & 1u;
+    // ---- phase A: window passes; the first also takes the warp frontier
+    bool first = true;
+    for (;;) {
+        const uint32_t ncl = min(ld_relaxed(&hx->cl_n[r % 3]), a.cap_cl);
+        const uint32_t nrc = min(ld_relaxed(&hx->rc_n[r % 3]), a.cap_l);
+        const uint32_t nrm = first ? min(ld_relaxed(&hx->rm_n[p]), a.V) : 0u;
+        if (ncl == 0 && nrm == 0 && nrc == 0) break;   // every thread reads the same counts
+        if (ex.lead) {
+            hx->cl_n[(r + 2) % 3] = 0;
+            hx->rc_n[(r + 2) % 3] = 0;
+        }
+        if (nrc <= 2 * ex.ncta) {
+            for (uint32_t i = ex.cta; i < nrc; i += ex.ncta) cta_entry(a, sh, p, r, __ldcg(a.rc[r % 3] + i));
+        } else {
+            // too many for one CTA each: window searches spread over every
+            // warp, from the next pass
+            for (uint32_t i = ex.gw * 32 + lane; i < nrc; i += ex.nw * 32) {
+                const uint32_t ent = __ldcg(a.rc[r % 3] + i), v = ent & ~kListFlag;
+                if (v < a.V) {
+                    const uint32_t d = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
+                    open_slot(a, p, r, v, __ldcg(a.est + v), d, false);
+                }
+            }
+        }
+        if (nrm) warp_batch(a, sh, st, p, r, a.rm[p], nrm, ex.wr, ex.nw);
+        for (uint32_t i = ex.wr; i < ncl; i += ex.nw) chunk_task(a, sh, st, p, r, __ldcg(a.cl[r % 3] + i), t == 1);
+        flush_bt(a, sh, st, p);
+        if (!hx_barrier(a, sh)) return -1;
+        ++r;
+        first = false;
+    }
+    // ---- phase B (sub-phase r)
+    if (ex.lead) {
+        hx->cl_n[(r + 2) % 3] = 0;
+        hx->rc_n[(r + 2) % 3] = 0;
+        hx->bt_n[p ^ 1u] = 0;
+        hx->rm_n[p] = 0;
+        hx->rl_n[p] = 0;
+    }
+    const uint32_t nbt = min(ld_relaxed(&hx->bt_n[p]), a.cap_bt);
+    update_tasks(a, sh, st, p, r, nbt, ex.wr, ex.nw);
+    if (!hx_barrier(a, sh)) return -1;
+    ++r;
+    const uint32_t nm = ld_relaxed(&hx->rm_n[p ^ 1u]), nl = ld_relaxed(&hx->rl_n[p ^ 1u]);
+    const uint32_t nc = ld_relaxed(&hx->rc_n[r % 3]);
+    if (nm == 0 && nl == 0 && nc == 0) return 1;
+    ++t;
+    if (t > a.max_iters) {   // the level peel takes over
+        if (ex.lead) hx->iters = t;
+        return 2;
+    }
+    return 0;
+}
+
 __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __grid_constant__ HxArgs a) {
     __shared__ HxShared sh;
     PeelCtl* ctl = a.ctl;
@@ -894,59 +963,11 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
     // (the first sweep queued chunk tasks into list (0 + 1) % 3 = 1, consumed at r = 1)
 
     uint32_t t = 1;
+    const Exec grid{blockIdx.x, gridDim.x, gw, wr, nw, lead};
     for (;;) {
-        const uint32_t p = t & 1u;
-        // ---- phase A: window passes; the first also takes the warp frontier
-        bool first = true;
-        for (;;) {
-            const uint32_t ncl = min(ld_relaxed(&hx->cl_n[r % 3]), a.cap_cl);
-            const uint32_t nrc = min(ld_relaxed(&hx->rc_n[r % 3]), a.cap_l);
-            const uint32_t nrm = first ? min(ld_relaxed(&hx->rm_n[p]), a.V) : 0u;
-            if (ncl == 0 && nrm == 0 && nrc == 0) break;   // every CTA reads the same counts
-            if (lead) {
-                hx->cl_n[(r + 2) % 3] = 0;
-                hx->rc_n[(r + 2) % 3] = 0;
-            }
-            if (nrc <= 2 * gridDim.x) {
-                for (uint32_t i = blockIdx.x; i < nrc; i += gridDim.x) cta_entry(a, sh, p, r, __ldcg(a.rc[r % 3] + i));
-            } else {
-                // too many for one CTA each: window searches spread over every
-                // warp, from the next pass
-                for (uint32_t i = gw * 32 + lane; i < nrc; i += nw * 32) {
-                    const uint32_t ent = __ldcg(a.rc[r % 3] + i), v = ent & ~kListFlag;
-                    if (v < a.V) {
-                        const uint32_t d = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
-                        open_slot(a, p, r, v, __ldcg(a.est + v), d, false);
-                    }
-                }
-            }
-            if (nrm) warp_batch(a, sh, st, p, r, a.rm[p], nrm, wr, nw);
-            for (uint32_t i = wr; i < ncl; i += nw) chunk_task(a, sh, st, p, r, __ldcg(a.cl[r % 3] + i), t == 1);
-            flush_bt(a, sh, st, p);
-            if (!hx_barrier(a, sh)) return;
-            ++r;
-            first = false;
-        }
-        // ---- phase B (sub-phase r)
-        if (lead) {
-            hx->cl_n[(r + 2) % 3] = 0;
-            hx->rc_n[(r + 2) % 3] = 0;
-            hx->bt_n[p ^ 1u] = 0;
-            hx->rm_n[p] = 0;
-            hx->rl_n[p] = 0;
-        }
-        const uint32_t nbt = min(ld_relaxed(&hx->bt_n[p]), a.cap_bt);
-        update_tasks(a, sh, st, p, r, nbt, wr, nw);
-        if (!hx_barrier(a, sh)) return;
-        ++r;
-        const uint32_t nm = ld_relaxed(&hx->rm_n[p ^ 1u]), nl = ld_relaxed(&hx->rl_n[p ^ 1u]);
-        const uint32_t nc = ld_relaxed(&hx->rc_n[r % 3]);
-        if (nm == 0 && nl == 0 && nc == 0) break;
-        ++t;
-        if (t > a.max_iters) {   // the level peel takes over
-            if (lead) hx->iters = t;
-            return;
-        }
+        const int state = hx_iteration(a, sh, st, t, r, grid);
+        if (state == 1) break;
+        if (state != 0) return;   // an error, or the budget: the level peel takes over
     }
 
     // Converged: est holds the core numbers.
