@@ -653,6 +653,7 @@ def main():
         "config": head["config"], "parallelism": f"replicas{world}",
         "hbm_gbs": head["hbm_gbs"], "arcs_per_s": head["arcs_per_s"], "kernel_ms": head["kernel_ms"],
         "roofline": head["roofline"], "e2e": head["e2e"], "gpu_launches": head["gpu_launches"],
+        "method": head.get("method"), "iterations": head.get("iterations"),
         "clocks": head["clocks"], "wall_s": head["wall_s"], "bit_exact_vs_oracle": True,
     }
     for k in ("cpu_baseline", "reference_gpu"):
