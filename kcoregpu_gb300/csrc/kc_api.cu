@@ -235,6 +235,21 @@ bool hindex_default() {
     return on;
 }
 
+// Where the h-index peel starts (KC_HX_START=n, read once per process): 0 =
+// from the degrees; n > 0 = after a level peel that stops at the first level
+// leaving at most V/n survivors, from their remaining degrees.
+uint32_t hindex_start() {
+    static uint32_t n = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (const char* e = std::getenv("KC_HX_START")) {
+            const long long x = std::atoll(e);
+            if (x >= 0 && x <= (1 << 20)) n = (uint32_t)x;
+        }
+    });
+    return n;
+}
+
 // Iterations after which the h-index peel gives the graph to the level peel
 // (KC_HX_ITERS, default 256): paths and long chains converge one hop per
 // iteration, where the level peel walks them in one level.
@@ -663,6 +678,25 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         h.max_iters = hindex_max_iters();
         h.wait_us = wait_limit_us();
         h.max_level = g->maxdeg;
+        h.w = g->d_w;
+        h.after_peel = 0;
+        if (const uint32_t n = hindex_start()) {
+            // The level peel's first levels, until at most V/n vertices survive
+            // (no tail hand-off).  It tags its task entries with its own epoch,
+            // so the fallback level peel below, which starts over, takes none
+            // of them for its own.
+            PeelArgs a0 = a;
+            a0.stop_alive = std::max<uint32_t>(1u, g->V / n);
+            a0.tail_cap_v = 0;
+            a0.epoch = g->epoch;
+            g->epoch = g->epoch % 255u + 1u;
+            if (g->epoch == 1u)
+                KC_CUDA(cudaMemsetAsync(g->d_tasks, 0, sizeof(unsigned long long) * g->task_cap, g->stream));
+            a.epoch = g->epoch;
+            void* a0args[] = {&a0};
+            KC_CUDA(cudaLaunchCooperativeKernel(peel_kernel(), dim3(g->grid), dim3(kPeelThreads), a0args, 0, g->stream));
+            h.after_peel = 1;
+        }
         void* hargs[] = {&h};
         KC_CUDA(cudaLaunchCooperativeKernel(peel_hindex_fn(), dim3(g->grid), dim3(kPeelThreads), hargs, 0, g->stream));
     }

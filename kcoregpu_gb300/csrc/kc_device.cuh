@@ -106,6 +106,9 @@ struct alignas(128) HxCtl {
     unsigned int tail_solved;  // 1: the cluster h-index tail found the survivors' core numbers
     unsigned int tail_iters;   // its iterations
     unsigned int pad7[30];
+    unsigned int peel_done;    // 1: a level peel finished every level (later peel launches return at once)
+    unsigned int stopped;      // 1: the level peel stopped early (PeelArgs::stop_alive) for the h-index
+    unsigned int pad8[30];
 };
 
 struct alignas(128) PeelCtl {
@@ -186,6 +189,11 @@ struct HxArgs {
     uint32_t max_iters;   // give up (the level peel runs instead) after this many iterations
     uint32_t wait_us;
     uint32_t max_level;   // 0xFFFFFFFF: the CSR was validated on the device (return if that failed)
+    // Start after a level peel that stopped early (HxCtl::stopped): w holds its
+    // states (claim bit and remaining degree + kBias) and est the core numbers
+    // of the peeled vertices; the survivors start from their remaining degree.
+    const uint32_t* w;
+    uint32_t after_peel;
 };
 
 struct PeelArgs {
@@ -232,6 +240,8 @@ struct PeelArgs {
     uint32_t chunk_arcs = kChunk;     // arcs per queued task, kMinChunk..kChunk
     uint32_t tail_hx_iters = 0;       // > 0: the cluster h-index tail (kc_hxtail.cu) runs first, for at most
                                       // this many iterations; the level tail kernel finishes otherwise
+    uint32_t stop_alive = 0;          // > 0: stop after the first level that leaves at most this many
+                                      // survivors (HxCtl::stopped), for the h-index peel to finish
 };
 
 // Tail peel: one CTA of kTailThreads threads, states in shared memory.

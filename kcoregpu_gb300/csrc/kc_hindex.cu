@@ -647,7 +647,15 @@ __device__ void chunk_task(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p
         xv[k] = 0;
         if (uu[k] < a.V) {
             const uint32_t u = uu[k];
-            const uint32_t x = degrees ? KC_LDG(a.off + u + 1) - KC_LDG(a.off + u) : __ldcg(a.est + u);
+            uint32_t x;
+            if (!degrees) {
+                x = __ldcg(a.est + u);
+            } else if (a.after_peel) {   // iteration 1 after a level peel: remaining degree or core number
+                const uint32_t wu = __ldcg(a.w + u);
+                x = (wu & kClaim) ? __ldcg(a.est + u) : wu - kBias;
+            } else {
+                x = KC_LDG(a.off + u + 1) - KC_LDG(a.off + u);
+            }
             xv[k] = x;
             bin[k] = x > hi ? 32u : (x >= lo ? (x - lo) >> shft : kNoBin);
         }
@@ -886,12 +894,22 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
     const uint32_t wr = wid * gridDim.x + blockIdx.x;
     const bool lead = blockIdx.x == 0 && threadIdx.x == 0;
     if (a.max_level == kFull && ld_err(&ctl->err)) return;   // the device validation refused the CSR
+    // after a level peel: nothing to do when it finished, or failed
+    if (a.after_peel && (ld_relaxed(&ctl->hx.peel_done) || !ld_relaxed(&ctl->hx.stopped) || ld_err(&ctl->err)))
+        return;
     if (threadIdx.x == 0) sh.bar_k = 0;
     Stager st;
 
-    // Sub-phase 0: est = degree, no active lists.
+    // Sub-phase 0: est = degree (after a level peel: a survivor's remaining
+    // degree; a peeled vertex keeps its core number, below every survivor's),
+    // no active lists.
     for (uint32_t v = gw * 32 + lane; v < a.V; v += nw * 32) {
-        a.est[v] = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
+        if (a.after_peel) {
+            const uint32_t x = __ldcg(a.w + v);
+            if (!(x & kClaim)) a.est[v] = x - kBias;
+        } else {
+            a.est[v] = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
+        }
         a.alen[v] = kFull;
     }
     if (!hx_barrier(a, sh)) return;
@@ -903,15 +921,22 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
     uint32_t r = 1;
     {
         for (uint32_t base = gw * 64; base < a.V; base += nw * 64) {
-            uint32_t vv[2], s0[2], d[2];
+            uint32_t vv[2], s0[2], d[2], e0[2];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 vv[h] = base + 32u * h + lane;
                 s0[h] = 0;
                 d[h] = 0;
+                e0[h] = 0;
                 if (vv[h] < a.V) {
                     s0[h] = KC_LDG(a.off + vv[h]);
                     d[h] = KC_LDG(a.off + vv[h] + 1) - s0[h];
+                    e0[h] = d[h];
+                    if (a.after_peel) {   // a peeled vertex takes no part; a survivor starts at its remaining degree
+                        const uint32_t x = __ldcg(a.w + vv[h]);
+                        if (x & kClaim) vv[h] = kFull;
+                        else e0[h] = x - kBias;
+                    }
                 }
             }
             uint32_t x[2][kHxLaneArcs];
@@ -928,11 +953,11 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
             }
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const uint32_t v = vv[h], dv = d[h];
+                const uint32_t v = vv[h], dv = d[h], ev = e0[h];
                 const bool small = v < a.V && dv <= kHxLaneArcs;
                 bool drop = false;
                 if (small) {
-                    uint32_t lo = 0, hi = dv;
+                    uint32_t lo = 0, hi = ev;
                     while (lo < hi) {
                         const uint32_t mid = (lo + hi + 1) >> 1;
                         uint32_t c = 0;
@@ -944,8 +969,8 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
 #pragma unroll
                     for (uint32_t i = 0; i < kHxLaneArcs; ++i) c += (i < dv && x[h][i] >= lo) ? 1u : 0u;
                     a.cnt[v] = c;
-                    if (lo < dv) {
-                        a.old[v] = dv;
+                    if (lo < ev) {
+                        a.old[v] = ev;
                         a.est[v] = lo;
                         drop = true;
                     }
@@ -953,7 +978,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
                 stage_bt(a, sh, st, 1, __ballot_sync(kFull, drop), (unsigned long long)v << 32);
                 const bool mid = v < a.V && dv > kHxLaneArcs && dv <= kHxWarpArcs;
                 stage_rm(a, sh, st, 1, __ballot_sync(kFull, mid), v);
-                if (v < a.V && dv > kHxWarpArcs) open_slot(a, 1, 0, v, dv, dv, true);
+                if (v < a.V && dv > kHxWarpArcs) open_slot(a, 1, 0, v, ev, dv, true);
             }
         }
         flush_bt(a, sh, st, 1);
@@ -967,7 +992,20 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
     for (;;) {
         const int state = hx_iteration(a, sh, st, t, r, grid);
         if (state == 1) break;
-        if (state != 0) return;   // an error, or the budget: the level peel takes over
+        if (state != 0) {   // an error, or the budget: the level peel takes over
+            if (state == 2 && lead && a.after_peel) {
+                // it starts over: the level counters the stopped level peel
+                // left behind go back to their initial values
+                for (int i = 0; i < 4; ++i) {
+                    LevelSlot* sl = &ctl->slot[i];
+                    sl->units_tail = 0; sl->head = 0; sl->peeled = 0; sl->arrived = 0;
+                    sl->alive_next = 0; sl->min_next = kFull; sl->arcs_next = 0;
+                }
+                ctl->iters_done = 0;
+                __threadfence();
+            }
+            return;
+        }
     }
 
     // Converged: est holds the core numbers.
@@ -977,7 +1015,7 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
     if (lane == 0 && mx) atomicMax(&ctl->kmax, mx);
     if (lead) {
         hx->iters = t;
-        ctl->iterations = t;
+        ctl->iterations = (a.after_peel ? ctl->iterations : 0u) + t;
         hx->solved = 1;
     }
 }

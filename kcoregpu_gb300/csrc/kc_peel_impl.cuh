@@ -1111,7 +1111,12 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
             if (a.shells && level + 1 < a.shell_cap) a.shells[level + 1] = peeled_total;
         }
         if (peeled_total >= a.V) {
-            if (lead) { ctl->kmax = level; ctl->levels = level + 1; ctl->iterations = it + 1; }
+            if (lead) {
+                ctl->kmax = level;
+                ctl->levels = level + 1;
+                ctl->iterations = it + 1;
+                ctl->hx.peel_done = 1;
+            }
             return;
         }
         if (level >= max_level) {
@@ -1125,6 +1130,16 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
         if (pi == 0 && mn != kFull && mn - kBias > next) next = mn - kBias;
         if (lead && a.shells)
             for (uint32_t l = level + 2; l <= next && l < a.shell_cap; ++l) a.shells[l] = peeled_total;
+        // Stop for the h-index peel once few vertices survive: every survivor
+        // has more than `level` surviving neighbours, so its core number is at
+        // least `next`, and its remaining degree is an upper bound of it.
+        if (a.stop_alive && a.V - peeled_total <= a.stop_alive) {
+            if (lead) {
+                ctl->hx.stopped = 1;
+                ctl->iterations = it + 1;
+            }
+            return;
+        }
         // Hand the rest to the tail peel once it fits: few survivors, and the
         // survivor degrees seen by this level's scans (an upper bound of the
         // induced arcs) plus padding within the tail's CSR capacity.
@@ -1168,8 +1183,9 @@ __device__ void peel_body(const PeelArgs& a, CtaShared& sh, uint32_t part, uint3
 
 __global__ void __launch_bounds__(kPeelThreads, 1) KC_PEEL_KERNEL(const __grid_constant__ PeelArgs a) {
     __shared__ CtaShared sh;
-    // the h-index peel launched before this kernel found every core number
-    if (ld_relaxed(&a.ctl->hx.solved)) return;
+    // the h-index peel launched before this kernel found every core number, or
+    // a level peel launched before it finished
+    if (ld_relaxed(&a.ctl->hx.solved) || ld_relaxed(&a.ctl->hx.peel_done)) return;
     peel_body(a, sh, blockIdx.x, gridDim.x);
 }
 #endif

@@ -3,7 +3,9 @@
 The level-peel settings are run with KC_ALGO=peel (the h-index peel, which
 runs first by default, would otherwise solve these graphs before the level
 peel starts); KC_ALGO=hindex runs the h-index peel, and KC_HX_ITERS=3 stops
-it early so that the level peel finishes from scratch.  With KC_TAIL=hindex
+it early so that the level peel finishes from scratch; KC_HX_START=8 starts
+the h-index after a level peel has left at most V/8 survivors (with
+KC_HX_ITERS=2 the level peel then starts over).  With KC_TAIL=hindex
 the survivors handed to the tail go to the cluster h-index tail (16-CTA
 cluster, estimates in distributed shared memory); with KC_HX_TAIL_ITERS=2 it
 gives up and the level tail finishes them.
@@ -69,6 +71,7 @@ LEVEL_PEEL = [
 
 @pytest.mark.parametrize("env", [{"KC_ALGO": "peel", **e} for e in LEVEL_PEEL] +
                          [{"KC_ALGO": "hindex"}, {"KC_ALGO": "hindex", "KC_HX_ITERS": "3"},
+                          {"KC_HX_START": "8"}, {"KC_HX_START": "8", "KC_HX_ITERS": "2"},
                           {"KC_ALGO": "peel", "KC_TAIL": "hindex"},
                           {"KC_ALGO": "peel", "KC_TAIL": "hindex", "KC_HX_TAIL_ITERS": "2"}],
                          ids=lambda e: ",".join(f"{k}={v}" for k, v in e.items()))
