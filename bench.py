@@ -370,10 +370,12 @@ def single_leg(cfg: int, args, torch, flush, local: int, world: int, steps: int,
                         "algorithmic_bytes": B,
                         "traffic": (NCU_TRAFFIC if st0["method"] == 1 else NCU_TRAFFIC_LEVEL_PEEL).get(cfg)},
            "method": "hindex" if st0["method"] == 1 else "level peel", "iterations": st0["iterations"],
-           # per step: the h-index kernel (h-index method), the persistent peel
-           # kernel and the tail kernel (both return at once after an h-index
-           # peel that converged)
-           "gpu_launches": (3 if st0["method"] == 1 else 2) * steps,
+           # per step: the h-index kernel and the cluster kernel it hands its
+           # last iterations to (h-index method; the cluster kernel is not
+           # launched with KC_HX_HANDOFF=0), the persistent peel kernel and the
+           # tail kernel (both return at once after an h-index peel that
+           # converged)
+           "gpu_launches": ((3 + (os.environ.get("KC_HX_HANDOFF", "1") != "0")) if st0["method"] == 1 else 2) * steps,
            "clocks": clk.summary(), "wall_s": t_wall, "bit_exact_vs_oracle": True}
     if args.profile:
         g.free()

@@ -143,6 +143,9 @@ struct kc_graph {
     unsigned long long* d_hx_cl[3] = {nullptr, nullptr, nullptr};
     uint32_t* d_hx_rc[3] = {nullptr, nullptr, nullptr};
     unsigned long long* d_hx_bt[2] = {nullptr, nullptr};
+    uint32_t* d_hx_tail = nullptr;  // hand-off to the cluster: estimates and counts of S (kTailV each)
+    uint32_t* d_hx_tnbr = nullptr;  // and its induced adjacency (spans as long as each member's source)
+    uint32_t hx_tnbr_cap = 0;
     uint32_t hx_cap_v = 0, hx_cap_l = 0, hx_cap_cl = 0, hx_cap_bt = 0;
     uint32_t method = KC_METHOD_AUTO;
 };
@@ -159,6 +162,8 @@ void release(kc_graph* g) {
     cudaFree(g->d_alive[0]); cudaFree(g->d_alive[1]);
     cudaFree(g->d_tail_ids); cudaFree(g->d_tail_off); cudaFree(g->d_tail_cur); cudaFree(g->d_tail_nbr);
     cudaFree(g->d_tail_items);
+    cudaFree(g->d_hx_tail);
+    cudaFree(g->d_hx_tnbr);
     cudaFree(g->d_hx_cnt); cudaFree(g->d_hx_old);
     cudaFree(g->d_hx_act); cudaFree(g->d_hx_alo); cudaFree(g->d_hx_alen);
     for (int i = 0; i < 2; ++i) { cudaFree(g->d_hx_slots[i]); cudaFree(g->d_hx_bins[i]); cudaFree(g->d_hx_bt[i]); }
@@ -367,6 +372,17 @@ int reserve_hx(kc_graph* g) {
         set_error_msg("graph too large for the h-index peel");
         return KC_ERR_OVERFLOW;
     }
+    if (!g->d_hx_tail) KC_CUDA(cudaMalloc(&g->d_hx_tail, sizeof(uint32_t) * 2 * kTailV));
+    {   // the hand-off's adjacency spans: up to every arc of the graph (at most 2^26), plus the quad padding
+        const uint64_t cap = ((std::min<uint64_t>(std::max<uint64_t>(E, 1), 1ull << 26) + 3ull * kTailV + 16) + 3) & ~3ull;
+        if (cap > g->hx_tnbr_cap) {
+            cudaFree(g->d_hx_tnbr);
+            g->d_hx_tnbr = nullptr;
+            g->hx_tnbr_cap = 0;
+            KC_CUDA(cudaMalloc(&g->d_hx_tnbr, sizeof(uint32_t) * cap));
+            g->hx_tnbr_cap = (uint32_t)cap;
+        }
+    }
     if (g->d_hx_cnt && g->hx_cap_v >= V && g->hx_cap_l >= cap_l && g->hx_cap_cl >= cap_cl && g->hx_cap_bt >= cap_bt)
         return KC_OK;
     cudaFree(g->d_hx_cnt); cudaFree(g->d_hx_old);
@@ -398,19 +414,12 @@ int reserve_hx(kc_graph* g) {
     return KC_OK;
 }
 
-// The cluster h-index tail (kc_hxtail.cu) on device `dev`: its shared-memory
-// and 16-CTA cluster opt-ins set, or null where such a cluster cannot run or
-// was not asked for: KC_TAIL=hindex (read once per process) sends the tails
-// to it; by default every tail goes to the level tail, which measured faster
-// on the benchmark graphs.
-const void* hxtail_kernel(int dev) {
+// The cluster h-index kernel (kc_hxtail.cu) on device `dev`: its
+// shared-memory and 16-CTA cluster opt-ins set, or null where such a cluster
+// cannot run.
+const void* hxcluster_kernel(int dev) {
     static std::mutex mu;
     static std::vector<int> state;   // 0 unknown, 1 usable, 2 not
-    static const bool off = [] {
-        const char* e = std::getenv("KC_TAIL");
-        return !(e && std::strcmp(e, "hindex") == 0);
-    }();
-    if (off) return nullptr;
     std::lock_guard<std::mutex> lk(mu);
     if ((int)state.size() <= dev) state.resize(dev + 1, 0);
     if (state[dev] == 0) {
@@ -437,6 +446,67 @@ const void* hxtail_kernel(int dev) {
         state[dev] = ok ? 1 : 2;
     }
     return state[dev] == 1 ? peel_hxtail_fn() : nullptr;
+}
+
+// The cluster kernel for the level peel's tails, or null: KC_TAIL=hindex
+// (read once per process) sends the tails to it; by default every tail goes
+// to the level tail, which measured faster on the benchmark graphs.
+const void* hxtail_kernel(int dev) {
+    static const bool on = [] {
+        const char* e = std::getenv("KC_TAIL");
+        return e && std::strcmp(e, "hindex") == 0;
+    }();
+    return on ? hxcluster_kernel(dev) : nullptr;
+}
+
+// The cluster kernel for the h-index peel's hand-off, or null: on by default,
+// KC_HX_HANDOFF=0 (read once per process) leaves every iteration to the
+// h-index kernel.
+const void* hxhandoff_kernel(int dev) {
+    static const bool on = [] {
+        const char* e = std::getenv("KC_HX_HANDOFF");
+        return !(e && std::strcmp(e, "0") == 0);
+    }();
+    return on ? hxcluster_kernel(dev) : nullptr;
+}
+
+// When the h-index peel tries the hand-off: once its frontier holds at most
+// KC_HX_HO_FRONT vertices (default 256), with S of at most KC_HX_HO_N
+// vertices (default and largest kTailV); read once per process.
+void handoff_limits(uint32_t& front, uint32_t& nmax) {
+    static uint32_t f = 256, m = kTailV;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        if (const char* e = std::getenv("KC_HX_HO_FRONT")) {
+            const long long x = std::atoll(e);
+            if (x >= 1 && x <= (1ll << 31)) f = (uint32_t)x;
+        }
+        if (const char* e = std::getenv("KC_HX_HO_N")) {
+            const long long x = std::atoll(e);
+            if (x >= 1 && x <= (long long)kTailV) m = (uint32_t)x;
+        }
+    });
+    front = f;
+    nmax = m;
+}
+
+// Launches the cluster kernel on the stream.
+int launch_hxcluster(const void* fn, PeelArgs* a, cudaStream_t stream) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(peel_hxtail_cluster());
+    cfg.blockDim = dim3(peel_hxtail_threads());
+    cfg.dynamicSmemBytes = peel_hxtail_smem();
+    cfg.stream = stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = peel_hxtail_cluster();
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    void* args[] = {a};
+    KC_CUDA(cudaLaunchKernelExC(&cfg, fn, args));
+    return KC_OK;
 }
 
 // Iterations after which the cluster h-index tail leaves the survivors to the
@@ -680,6 +750,19 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         h.max_level = g->maxdeg;
         h.w = g->d_w;
         h.after_peel = 0;
+        // the hand-off to the cluster kernel (not after a level peel, whose
+        // peeled vertices keep no counts)
+        const void* hof = (tail && !hindex_start()) ? hxhandoff_kernel(g->dev) : nullptr;
+        h.handoff = hof ? 1u : 0u;
+        h.lmap = g->d_hx_old;
+        h.tail_ids = g->d_tail_ids;
+        h.tail_off = g->d_tail_off;
+        h.tail_cur = g->d_tail_cur;
+        h.tail_nbr = g->d_hx_tnbr;
+        h.tail_est = g->d_hx_tail;
+        h.tail_cnt = g->d_hx_tail + kTailV;
+        h.tail_cap_arcs = g->hx_tnbr_cap;
+        handoff_limits(h.ho_front, h.ho_max);
         if (const uint32_t n = hindex_start()) {
             // The level peel's first levels, until at most V/n vertices survive
             // (no tail hand-off).  It tags its task entries with its own epoch,
@@ -699,6 +782,15 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         }
         void* hargs[] = {&h};
         KC_CUDA(cudaLaunchCooperativeKernel(peel_hindex_fn(), dim3(g->grid), dim3(kPeelThreads), hargs, 0, g->stream));
+        if (hof) {   // returns at once unless the h-index kernel handed over
+            PeelArgs ah = a;
+            ah.tail_est = h.tail_est;
+            ah.tail_cnt = h.tail_cnt;
+            ah.tail_nbr = h.tail_nbr;
+            ah.tail_hx_iters = hxtail_max_iters();
+            const int rc = launch_hxcluster(hof, &ah, g->stream);
+            if (rc) return rc;
+        }
     }
     // The survivors handed over go to the cluster h-index tail first (not for
     // the peel order or the per-level trace, which follow the level tail);
@@ -708,19 +800,8 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
     void* args[] = {&a};
     KC_CUDA(cudaLaunchCooperativeKernel(peel_kernel(), dim3(g->grid), dim3(kPeelThreads), args, 0, g->stream));
     if (hxt) {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(peel_hxtail_cluster());
-        cfg.blockDim = dim3(peel_hxtail_threads());
-        cfg.dynamicSmemBytes = peel_hxtail_smem();
-        cfg.stream = g->stream;
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = peel_hxtail_cluster();
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        KC_CUDA(cudaLaunchKernelExC(&cfg, hxt, args));
+        const int rc = launch_hxcluster(hxt, &a, g->stream);
+        if (rc) return rc;
     }
     if (tail)
         KC_CUDA(cudaLaunchKernel(tail_kernel(g->dev), dim3(1), dim3(kTailThreads), args, peel_tail_smem(), g->stream));

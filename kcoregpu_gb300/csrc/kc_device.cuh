@@ -109,6 +109,20 @@ struct alignas(128) HxCtl {
     unsigned int peel_done;    // 1: a level peel finished every level (later peel launches return at once)
     unsigned int stopped;      // 1: the level peel stopped early (PeelArgs::stop_alive) for the h-index
     unsigned int pad8[30];
+    // Hand-off of the h-index peel to the cluster tail (kc_hindex.cu try_handoff)
+    unsigned int handoff;      // 1: the set S below was handed over; the cluster tail finishes it
+    unsigned int ho_floor;     // T: every vertex of S has at least T neighbours in S
+    unsigned int ho_n;         // |S| (local ids 0 .. ho_n-1)
+    unsigned int pad9[29];
+    // counters of an attempt, by attempt parity (the lead clears the other
+    // parity's during an attempt, so no attempt needs a barrier to reset them)
+    unsigned int ho_min[2];      // smallest estimate of the frontier
+    unsigned int ho_cnt[2][5];   // vertices at or above each candidate floor
+    unsigned int ho_m[2];        // members given local ids
+    unsigned int ho_fail[2];     // a member has fewer than T neighbours in S, or a buffer is too small
+    unsigned int ho_tasks[2];    // chunk tasks over the members' sources
+    unsigned int ho_arcs[2];     // induced-CSR entries reserved (each member: its source length, padded to quads)
+    unsigned int pad10[12];
 };
 
 struct alignas(128) PeelCtl {
@@ -194,6 +208,21 @@ struct HxArgs {
     // of the peeled vertices; the survivors start from their remaining degree.
     const uint32_t* w;
     uint32_t after_peel;
+    // Hand-off to the cluster tail (handoff != 0): the induced CSR of S with
+    // local ids, in the tail buffers of the level peel (kTailV vertices), plus
+    // S's estimates and counts by local id; lmap (V entries; may be `old`,
+    // which holds nothing between iterations) maps a vertex to its local id.
+    uint32_t handoff;
+    uint32_t* lmap;
+    uint32_t* tail_ids;
+    uint32_t* tail_off;
+    uint32_t* tail_cur;
+    uint32_t* tail_nbr;
+    uint32_t* tail_est;
+    uint32_t* tail_cnt;
+    uint32_t tail_cap_arcs;
+    uint32_t ho_front;   // try the hand-off once the frontier holds at most this many vertices
+    uint32_t ho_max;     // and S at most this many (<= kTailV)
 };
 
 struct PeelArgs {
@@ -242,6 +271,8 @@ struct PeelArgs {
                                       // this many iterations; the level tail kernel finishes otherwise
     uint32_t stop_alive = 0;          // > 0: stop after the first level that leaves at most this many
                                       // survivors (HxCtl::stopped), for the h-index peel to finish
+    uint32_t* tail_est = nullptr;     // h-index hand-off: estimates and counts of S by local id
+    uint32_t* tail_cnt = nullptr;
 };
 
 // Tail peel: one CTA of kTailThreads threads, states in shared memory.

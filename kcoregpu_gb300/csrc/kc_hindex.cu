@@ -883,6 +883,251 @@ __device__ int hx_iteration(const HxArgs& a, HxShared& sh, Stager& st, uint32_t&
     return 0;
 }
 
+// ------------------------------------------------------------ cluster hand-off
+// Late iterations touch few vertices but each still costs two or three grid
+// barriers and their chains of L2 round trips; a 16-CTA cluster runs them
+// about twice as fast (kc_hxtail.cu).  The set handed over is S = {v : est[v]
+// >= T} with T at most the smallest estimate in the next frontier, so that
+// every queued vertex is in S.  The hand-off is made only when every vertex
+// of S has at least T neighbours in S: S then lies in the T-core, so every
+// core number in S is at least T and no estimate in S falls below T; the
+// vertices outside S, none of them queued and none of them ever crossed by a
+// drop in S (their estimates are below T), are final.  Inside S the counts
+// stay valid (every neighbour they count has an estimate >= est >= T).  The
+// cluster continues the same iteration on the induced CSR of S from these
+// estimates and counts.  T is the smallest of T0/2, 5T0/8, ... T0 (T0 the
+// frontier's smallest estimate) that leaves at most kTailV vertices in S.
+
+constexpr uint32_t kHoMark = 0xFFFFFFFEu;   // lmap: a queued vertex (before the local ids are given)
+constexpr uint32_t kHoTask = 256;           // entries per chunk task of the hand-off
+constexpr int kHoCand = 5;                  // candidate floors
+
+__device__ __forceinline__ uint32_t cand_floor(uint32_t T0, int k) {
+    return max(1u, (uint32_t)(((unsigned long long)T0 * (4u + k)) / 8u));
+}
+
+// Visits the next frontier (iteration t, sub-phase r): f(v) per queued vertex.
+template <class F>
+__device__ __forceinline__ void for_frontier(const HxArgs& a, uint32_t t, uint32_t r, uint32_t gw, uint32_t nw, F f) {
+    HxCtl* hx = &a.ctl->hx;
+    const unsigned lane = lane_id();
+    const uint32_t q = t & 1u;
+    const uint32_t nm = min(ld_relaxed(&hx->rm_n[q]), a.V), nl = min(ld_relaxed(&hx->rl_n[q]), a.cap_l);
+    const uint32_t nc = min(ld_relaxed(&hx->rc_n[r % 3]), a.cap_l);
+    for (uint32_t base = gw * 32; base < nm + nl + nc; base += nw * 32) {   // warp-uniform
+        const uint32_t i = base + lane;
+        uint32_t v = kFull;
+        if (i < nm) v = __ldcg(a.rm[q] + i) & ~kListFlag;
+        else if (i < nm + nl) v = __ldcg(&a.slots[q][i - nm].v);
+        else if (i < nm + nl + nc) v = __ldcg(a.rc[r % 3] + (i - nm - nl)) & ~kListFlag;
+        f(v < a.V ? v : kFull);
+    }
+}
+
+// A chunk task of the hand-off: the low word is the position of its first
+// entry in the member's source (the adjacency, or its active list when that
+// is complete for the floor: the vertex is not queued, so no window pass is
+// rebuilding it, and its list floor is at or below T); the high word holds
+// the member's local id (bits 0-14), the source (bit 15: the list) and the
+// entry count - 1 (bits 16-23).
+constexpr uint32_t kHoListed = 1u << 15;
+
+// A task's entries, 8 a lane, all loads in flight; u = 0xFFFFFFFF past the end.
+__device__ __forceinline__ void ho_load(const HxArgs& a, unsigned long long tk, uint32_t& lid,
+                                        uint32_t (&u)[kHoTask / 32]) {
+    const unsigned lane = lane_id();
+    const uint32_t hi = (uint32_t)(tk >> 32), pos = (uint32_t)tk;
+    lid = hi & 0x7FFFu;
+    const bool listed = (hi & kHoListed) != 0;
+    const uint32_t m = ((hi >> 16) & 0xFFu) + 1u;
+#pragma unroll
+    for (uint32_t j = 0; j < kHoTask / 32; ++j) {
+        const uint32_t x = 32u * j + lane;
+        u[j] = x < m ? (listed ? __ldcg(a.act + pos + x) : KC_LDG(a.nbr + pos + x)) : kFull;
+    }
+}
+
+// Builds the induced CSR of S (local ids; each adjacency in a span as long as
+// its source, padded to quads) in the tail buffers and checks that every
+// member has at least T neighbours in S.  Returns 1 when S is handed over, 0
+// when no floor leaves S small enough, 2 when S failed the certificate (or
+// did not fit), -1 on a failed barrier; the grid goes on after 0 and 2.
+// Every CTA calls it with the same attempt number k.
+__device__ int try_handoff(const HxArgs& a, HxShared& sh, uint32_t t, uint32_t r, uint32_t k, const Exec& ex) {
+    HxCtl* hx = &a.ctl->hx;
+    const unsigned lane = lane_id();
+    const uint32_t P = k & 1u;
+    unsigned long long* tasks = a.bt[t & 1u];   // both update-task lists are free between iterations
+    constexpr uint32_t kU = kHoTask / 32;
+    // 0: the frontier's smallest estimate; queued vertices marked in lmap
+    {
+        uint32_t mn = kFull;
+        for_frontier(a, t, r, ex.gw, ex.nw, [&](uint32_t v) {
+            if (v != kFull) {
+                mn = min(mn, __ldcg(a.est + v));
+                a.lmap[v] = kHoMark;
+            }
+        });
+        mn = __reduce_min_sync(kFull, mn);
+        if (lane == 0 && mn != kFull) atomicMin(&hx->ho_min[P], mn);
+    }
+    if (!hx_barrier(a, sh)) return -1;
+    if (ex.lead) {   // the next attempt's counters (no CTA touches them until then)
+        hx->ho_min[P ^ 1u] = kFull;
+        for (int c = 0; c < kHoCand; ++c) hx->ho_cnt[P ^ 1u][c] = 0;
+        hx->ho_m[P ^ 1u] = 0;
+        hx->ho_fail[P ^ 1u] = 0;
+        hx->ho_tasks[P ^ 1u] = 0;
+        hx->ho_arcs[P ^ 1u] = 0;
+    }
+    const uint32_t T0 = ld_relaxed(&hx->ho_min[P]);
+    if (T0 == kFull || T0 < 2) return 0;
+    // 1: |S| for each candidate floor
+    {
+        uint32_t c[kHoCand] = {};
+        uint32_t fl[kHoCand];
+#pragma unroll
+        for (int j = 0; j < kHoCand; ++j) fl[j] = cand_floor(T0, j);
+        for (uint32_t base = ex.gw * 32 * kU; base < a.V; base += ex.nw * 32 * kU) {
+            uint32_t e[kU];
+#pragma unroll
+            for (uint32_t u = 0; u < kU; ++u) {
+                const uint32_t v = base + 32u * u + lane;
+                e[u] = v < a.V ? __ldcg(a.est + v) : 0u;
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < kU; ++u)
+#pragma unroll
+                for (int j = 0; j < kHoCand; ++j) c[j] += e[u] >= fl[j] ? 1u : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < kHoCand; ++j) {
+            const uint32_t x = __reduce_add_sync(kFull, c[j]);
+            if (lane == 0 && x) atomicAdd(&hx->ho_cnt[P][j], x);
+        }
+    }
+    if (!hx_barrier(a, sh)) return -1;
+    int pick = -1;
+    const uint32_t nmax = min(a.ho_max, kTailV);
+    for (int j = 0; j < kHoCand && pick < 0; ++j) {
+        const uint32_t x = ld_relaxed(&hx->ho_cnt[P][j]);
+        if (x > 0 && x <= nmax) pick = j;
+    }
+    if (pick < 0) return 0;
+    const uint32_t T = cand_floor(T0, pick), n = ld_relaxed(&hx->ho_cnt[P][pick]);
+    // 2: members: local ids, estimates, counts (a queued vertex's as zero: it
+    // may have been taken below zero by decrements of neighbours it had not
+    // counted, and zero queues it in the cluster too), spans, chunk tasks
+    for (uint32_t base = ex.gw * 32 * kU; base < a.V; base += ex.nw * 32 * kU) {   // warp-uniform
+        uint32_t e[kU];
+#pragma unroll
+        for (uint32_t u = 0; u < kU; ++u) {
+            const uint32_t v = base + 32u * u + lane;
+            e[u] = v < a.V ? __ldcg(a.est + v) : 0u;
+        }
+#pragma unroll
+        for (uint32_t u = 0; u < kU; ++u) {
+            const uint32_t v = base + 32u * u + lane;
+            const bool in = v < a.V && e[u] >= T;
+            const unsigned m = __ballot_sync(kFull, in);
+            if (!m) continue;
+            uint32_t s0 = 0, len = 0, tag = 0;
+            bool queued = false;
+            if (in) {
+                queued = __ldcg(a.lmap + v) == kHoMark;
+                s0 = KC_LDG(a.off + v);
+                const uint32_t d = KC_LDG(a.off + v + 1) - s0;
+                len = d;
+                if (!queued) {
+                    const uint32_t al = __ldcg(a.alen + v);
+                    if (al != kFull && __ldcg(a.alo + v) <= T) {
+                        len = min(al, d);
+                        tag = kHoListed;
+                    }
+                }
+            }
+            const uint32_t nch = (len + kHoTask - 1) / kHoTask, span = (len + 3u) & ~3u;
+            uint32_t ntot, stot;
+            const uint32_t cex = warp_excl_scan(nch, &ntot);
+            const uint32_t sex = warp_excl_scan(span, &stot);
+            uint32_t b = 0, tb = 0, ab = 0;
+            if (lane == 0) {
+                b = atomicAdd(&hx->ho_m[P], (uint32_t)__popc(m));
+                if (ntot) tb = atomicAdd(&hx->ho_tasks[P], ntot);
+                if (stot) ab = atomicAdd(&hx->ho_arcs[P], stot);
+            }
+            b = __shfl_sync(kFull, b, 0);
+            tb = __shfl_sync(kFull, tb, 0) + cex;
+            ab = __shfl_sync(kFull, ab, 0) + sex;
+            if (in) {
+                const uint32_t lid = b + __popc(m & lanemask_lt());
+                if (lid < n && ab + span <= a.tail_cap_arcs && tb + nch <= a.cap_bt) {
+                    a.lmap[v] = lid;
+                    a.tail_ids[lid] = v;
+                    a.tail_est[lid] = e[u];
+                    a.tail_cnt[lid] = queued ? 0u : __ldcg(a.cnt + v);
+                    a.tail_off[lid] = ab;
+                    a.tail_cur[lid] = ab;
+                    for (uint32_t c = 0; c < nch; ++c) {
+                        const uint32_t cnt = min(kHoTask, len - c * kHoTask);
+                        tasks[tb + c] = ((unsigned long long)(lid | tag | ((cnt - 1u) << 16)) << 32) |
+                                        (s0 + c * kHoTask);
+                    }
+                } else {
+                    atomicOr(&hx->ho_fail[P], 1u);
+                }
+            }
+        }
+    }
+    if (!hx_barrier(a, sh)) return -1;
+    if (ld_relaxed(&hx->ho_fail[P])) return 2;
+    const uint32_t ntask = min(ld_relaxed(&hx->ho_tasks[P]), a.cap_bt);
+    // 3: each member's neighbours in S as local ids, appended to its span
+    for (uint32_t i = ex.wr; i < ntask; i += ex.nw) {
+        uint32_t lid, u[kU];
+        ho_load(a, __ldcg(tasks + i), lid, u);
+        uint32_t x[kU];
+#pragma unroll
+        for (uint32_t j = 0; j < kU; ++j) x[j] = u[j] < a.V ? __ldcg(a.est + u[j]) : 0u;
+#pragma unroll
+        for (uint32_t j = 0; j < kU; ++j) x[j] = (u[j] < a.V && x[j] >= T) ? __ldcg(a.lmap + u[j]) : kFull;
+        uint32_t c = 0;
+#pragma unroll
+        for (uint32_t j = 0; j < kU; ++j) c += x[j] < n ? 1u : 0u;
+        uint32_t tot;
+        const uint32_t cx = warp_excl_scan(c, &tot);
+        if (tot == 0 || lid >= n) continue;
+        uint32_t pb = 0;
+        if (lane == 0) pb = atomicAdd(a.tail_cur + lid, tot);
+        uint32_t at = __shfl_sync(kFull, pb, 0) + cx;
+#pragma unroll
+        for (uint32_t j = 0; j < kU; ++j) {
+            if (x[j] < n) {
+                if (at < a.tail_cap_arcs) a.tail_nbr[at] = x[j];
+                else atomicOr(&hx->ho_fail[P], 1u);
+                ++at;
+            }
+        }
+    }
+    if (!hx_barrier(a, sh)) return -1;
+    // 4: the certificate; the pads after each adjacency
+    for (uint32_t i = ex.gw * 32 + lane; i < n; i += ex.nw * 32) {
+        const uint32_t o = __ldcg(a.tail_off + i), end = __ldcg(a.tail_cur + i);
+        if (end - o < T) atomicOr(&hx->ho_fail[P], 1u);
+        for (uint32_t q = end; q < ((end + 3u) & ~3u) && q < a.tail_cap_arcs; ++q) a.tail_nbr[q] = kFull;
+    }
+    if (ex.lead) a.ctl->tail_arcs = min(ld_relaxed(&hx->ho_arcs[P]), a.tail_cap_arcs);
+    if (!hx_barrier(a, sh)) return -1;
+    if (ld_relaxed(&hx->ho_fail[P])) return 2;
+    if (ex.lead) {
+        hx->ho_floor = T;
+        hx->ho_n = n;
+        hx->iters = t - 1;
+        hx->handoff = 1;
+    }
+    return 1;
+}
+
 __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __grid_constant__ HxArgs a) {
     __shared__ HxShared sh;
     PeelCtl* ctl = a.ctl;
@@ -898,6 +1143,14 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
     if (a.after_peel && (ld_relaxed(&ctl->hx.peel_done) || !ld_relaxed(&ctl->hx.stopped) || ld_err(&ctl->err)))
         return;
     if (threadIdx.x == 0) sh.bar_k = 0;
+    if (lead) {   // the first hand-off attempt's counters (seen by every CTA after the first barrier)
+        hx->ho_min[0] = kFull;
+        for (int c = 0; c < kHoCand; ++c) hx->ho_cnt[0][c] = 0;
+        hx->ho_m[0] = 0;
+        hx->ho_fail[0] = 0;
+        hx->ho_tasks[0] = 0;
+        hx->ho_arcs[0] = 0;
+    }
     Stager st;
 
     // Sub-phase 0: est = degree (after a level peel: a survivor's remaining
@@ -989,8 +1242,22 @@ __global__ void __launch_bounds__(kPeelThreads, 1) peel_hindex_kernel(const __gr
 
     uint32_t t = 1;
     const Exec grid{blockIdx.x, gridDim.x, gw, wr, nw, lead};
+    // hand-off attempts: every other iteration while no floor leaves S small
+    // enough; after a failed certificate, twice as long a wait each time
+    uint32_t last_try = 0, attempts = 0, gap = 2;
     for (;;) {
         const int state = hx_iteration(a, sh, st, t, r, grid);
+        if (state == 0 && a.handoff && t >= 3 && t >= last_try + gap) {
+            // (every CTA reads the same counts after the iteration's last barrier)
+            const uint32_t nf = min(ld_relaxed(&hx->rm_n[t & 1u]), a.V) + min(ld_relaxed(&hx->rl_n[t & 1u]), a.cap_l) +
+                                min(ld_relaxed(&hx->rc_n[r % 3]), a.cap_l);
+            if (nf <= a.ho_front) {
+                last_try = t;
+                const int ho = try_handoff(a, sh, t, r, attempts++, grid);
+                if (ho == 1 || ho < 0) return;   // handed over, or an error
+                if (ho == 2) gap *= 2;
+            }
+        }
         if (state == 1) break;
         if (state != 0) {   // an error, or the budget: the level peel takes over
             if (state == 2 && lead && a.after_peel) {

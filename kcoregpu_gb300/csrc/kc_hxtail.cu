@@ -28,6 +28,13 @@
 // After max iterations without convergence the kernel leaves the survivors
 // to the level tail kernel, launched after it, which returns at once when
 // this kernel set HxCtl::tail_solved.
+//
+// The same kernel finishes the h-index peel (kc_hindex.cu try_handoff): there
+// S is the set of vertices whose estimates are at or above a floor T that the
+// h-index peel certified (every member has at least T neighbours in S), the
+// induced CSR is built by that kernel, and the iteration continues from its
+// estimates, counts and queued vertices.  After max iterations without
+// convergence the level peel runs from the start instead.
 #include <cooperative_groups.h>
 
 #include "kc_device.cuh"
@@ -293,7 +300,9 @@ struct Tail {
 
     // Phase A for the big slots: their estimates gathered together (all
     // threads, four quads in flight each) while they fit kCVals values, then
-    // each h-index with CTA reductions; a slot above kCVals arcs alone.
+    // the h-indexes, a warp each when the batch holds four or more slots,
+    // else one after the other with CTA reductions; a slot above kCVals arcs
+    // alone.
     __device__ void recompute_big() {
         big_prefix();
         const unsigned tid = threadIdx.x;
@@ -342,17 +351,34 @@ struct Tail {
                 }
             }
             __syncthreads();
-            for (uint32_t i = i0; i < i1; ++i) {
-                const uint32_t sl = sm.big[i], off = sm.bv[i] - v0, d = sm.bv[i + 1] - sm.bv[i];
-                const uint32_t e = sm.eall[vertex(sl)];
-                auto ge = [&](uint32_t h) {
-                    uint32_t c = 0;
-                    for (uint32_t j = tid; j < d; j += kClThreads) c += sm.vals[off + j] >= h ? 1u : 0u;
-                    return cl_sum(c, sm);
-                };
-                const uint32_t h = tail_gallop(ge, L, e);
-                const uint32_t c = ge(h);
-                if (tid == 0) result(sl, e, h, c);
+            if (i1 - i0 >= 4) {   // several slots: a warp each
+                const unsigned lane = lane_id(), wid = tid >> 5;
+                for (uint32_t i = i0 + wid; i < i1; i += kClWarps) {   // warp-uniform
+                    const uint32_t sl = sm.big[i], d = sm.bv[i + 1] - sm.bv[i];
+                    const uint32_t* xs = sm.vals + (sm.bv[i] - v0);
+                    const uint32_t e = sm.eall[vertex(sl)];
+                    auto ge = [&](uint32_t h) {
+                        uint32_t c = 0;
+                        for (uint32_t j = lane; j < d; j += 32) c += xs[j] >= h ? 1u : 0u;
+                        return __reduce_add_sync(kFull, c);
+                    };
+                    const uint32_t h = tail_gallop(ge, L, e);
+                    const uint32_t c = ge(h);
+                    if (lane == 0) result(sl, e, h, c);
+                }
+            } else {
+                for (uint32_t i = i0; i < i1; ++i) {
+                    const uint32_t sl = sm.big[i], off = sm.bv[i] - v0, d = sm.bv[i + 1] - sm.bv[i];
+                    const uint32_t e = sm.eall[vertex(sl)];
+                    auto ge = [&](uint32_t h) {
+                        uint32_t c = 0;
+                        for (uint32_t j = tid; j < d; j += kClThreads) c += sm.vals[off + j] >= h ? 1u : 0u;
+                        return cl_sum(c, sm);
+                    };
+                    const uint32_t h = tail_gallop(ge, L, e);
+                    const uint32_t c = ge(h);
+                    if (tid == 0) result(sl, e, h, c);
+                }
             }
             __syncthreads();
             i0 = i1;
@@ -531,18 +557,28 @@ __global__ void __launch_bounds__(kClThreads, 1) peel_hxtail_kernel(const __grid
     PeelCtl* ctl = a.ctl;
     const unsigned tid = threadIdx.x;
     // every CTA of the cluster takes the same exit here, before any barrier
-    const uint32_t n = ctl->tail_n;
-    if (n == 0 || ctl->err != 0 || n > kTailV || n > a.tail_cap_v || a.tail_hx_iters == 0) return;
-    Tail T{a, sm, cl, n, ctl->tail_level, (uint32_t)cl.block_rank(), ctl->tail_arcs / 4u,
+    const bool ho = a.tail_est != nullptr;   // the launch after the h-index peel (hand-off mode)
+    if (ctl->err != 0 || a.tail_hx_iters == 0 || (ho && ctl->hx.handoff == 0)) return;
+    const uint32_t n = ho ? ctl->hx.ho_n : ctl->tail_n;
+    if (n == 0 || n > kTailV || (!ho && n > a.tail_cap_v)) return;
+    Tail T{a, sm, cl, n, ho ? ctl->hx.ho_floor : ctl->tail_level, (uint32_t)cl.block_rank(), ctl->tail_arcs / 4u,
            reinterpret_cast<const uint4*>(a.tail_nbr)};
     const uint32_t own = n > T.rank ? (n - T.rank + kCl - 1) / kCl : 0u;
-    for (uint32_t v = tid; v < kTailV; v += kClThreads) sm.eall[v] = v < n ? T.degree(v) : 0u;
-    for (uint32_t s = tid; s < kPer; s += kClThreads) sm.cnt[s] = 0;
+    // level tail: estimates from the induced degrees, every vertex in the first
+    // frontier; hand-off: the h-index peel's estimates and counts, its queued
+    // vertices (a count below the estimate) in the first frontier
+    for (uint32_t v = tid; v < kTailV; v += kClThreads)
+        sm.eall[v] = v < n ? (ho ? __ldcg(a.tail_est + v) : T.degree(v)) : 0u;
+    for (uint32_t s = tid; s < kPer; s += kClThreads) sm.cnt[s] = ho && s < own ? __ldcg(a.tail_cnt + T.vertex(s)) : 0u;
     for (uint32_t w = tid; w < 2 * (kPer / 32); w += kClThreads) (&sm.front[0][0])[w] = 0;
     if (tid == 0) {
         sm.flag[0] = sm.flag[1] = sm.flag[2] = 0;
         sm.kmax = 0;
     }
+    __syncthreads();
+    if (ho)
+        for (uint32_t s = tid; s < own; s += kClThreads)
+            if (sm.cnt[s] < sm.eall[T.vertex(s)]) atomicOr(&sm.front[1][s >> 5], 1u << (s & 31));
     cl.sync();
 
     bool solved = false;
@@ -554,7 +590,7 @@ __global__ void __launch_bounds__(kClThreads, 1) peel_hxtail_kernel(const __grid
         if (T.rank == 0 && tid == 0) sm.flag[(t + 1) % 3] = 0;
         __syncthreads();
         for (uint32_t s = tid; s < own; s += kClThreads) {
-            const bool in = t == 1 || ((sm.front[p][s >> 5] >> (s & 31)) & 1u);
+            const bool in = (t == 1 && !ho) || ((sm.front[p][s >> 5] >> (s & 31)) & 1u);
             if (!in) continue;
             if (T.degree(T.vertex(s)) <= kWVals) sm.work[atomicAdd(&sm.nwork, 1u)] = s;
             else sm.big[atomicAdd(&sm.nbig, 1u)] = s;
@@ -597,9 +633,14 @@ __global__ void __launch_bounds__(kClThreads, 1) peel_hxtail_kernel(const __grid
     if (solved && T.rank == 0 && tid == 0) {
         ctl->kmax = sm.kmax;
         ctl->levels = sm.kmax + 1;
-        ctl->iterations = ctl->tail_iter + t;
-        ctl->hx.tail_solved = 1;
         ctl->hx.tail_iters = t;
+        if (ho) {   // the vertices outside S kept their final estimates
+            ctl->iterations = ctl->hx.iters + t;
+            ctl->hx.solved = 1;
+        } else {
+            ctl->iterations = ctl->tail_iter + t;
+            ctl->hx.tail_solved = 1;
+        }
     }
     cl.sync();   // no CTA leaves while another may still read its shared memory
 }

@@ -144,7 +144,7 @@ def test_path_falls_back_to_the_level_peel(gpu):
 
 def _child(code, **env):
     e = dict(os.environ)
-    for k in ("KC_ALGO", "KC_HX_ITERS"):
+    for k in ("KC_ALGO", "KC_HX_ITERS", "KC_HX_HANDOFF", "KC_HX_HO_FRONT", "KC_HX_HO_N", "KC_HX_TAIL_ITERS"):
         e.pop(k, None)
     e.update({k: str(v) for k, v in env.items()})
     pre = f"import sys, json; sys.path.insert(0, {str(ROOT)!r})\nimport numpy as np\nimport kcoregpu_gb300 as kc\nfrom oracle import kc_oracle as O\n"
