@@ -228,7 +228,8 @@ __device__ __forceinline__ void push_cta(const HxArgs& a, uint32_t r, uint32_t e
 
 // The window of a large vertex queued for recomputation: its active list from
 // the top 32 values down (when it has one), else the adjacency, from [0, e]
-// when coarse (iteration 1, where estimates fall far) or the top 32 values.
+// when coarse (iterations 1 and 2, where estimates fall far) or the top 32
+// values.
 __device__ void open_slot(const HxArgs& a, uint32_t q, uint32_t r, uint32_t v, uint32_t e, uint32_t d, bool coarse) {
     const uint32_t al = coarse ? kFull : __ldcg(a.alen + v);
     const uint32_t l0 = coarse ? 0u : __ldcg(a.alo + v);
@@ -711,7 +712,7 @@ __device__ void chunk_task(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p
 // whose estimate x satisfies new < x <= old loses one count; the decrement
 // that takes its count below x queues it.
 __device__ void update_tasks(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p, uint32_t r, uint32_t nbt,
-                             uint32_t wr, uint32_t nw) {
+                             uint32_t wr, uint32_t nw, bool coarse) {
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     const uint32_t q = p ^ 1u;
     // per-warp task table in the (free) bin area: prefix, first arc, old, new
@@ -801,7 +802,7 @@ __device__ void update_tasks(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
                         } else {
                             if (usable && al <= kHxCtaVals) push_cta(a, r, wv[j] | kListFlag);
                             else if (!usable && dq <= kHxCtaVals) push_cta(a, r, wv[j]);
-                            else open_slot(a, q, r, wv[j], xv[j], dq, false);
+                            else open_slot(a, q, r, wv[j], xv[j], dq, coarse);
                             queue = false;
                         }
                     }
@@ -849,7 +850,7 @@ __device__ int hx_iteration(const HxArgs& a, HxShared& sh, Stager& st, uint32_t&
                 const uint32_t ent = __ldcg(a.rc[r % 3] + i), v = ent & ~kListFlag;
                 if (v < a.V) {
                     const uint32_t d = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
-                    open_slot(a, p, r, v, __ldcg(a.est + v), d, false);
+                    open_slot(a, p, r, v, __ldcg(a.est + v), d, t == 2);
                 }
             }
         }
@@ -869,7 +870,9 @@ __device__ int hx_iteration(const HxArgs& a, HxShared& sh, Stager& st, uint32_t&
         hx->rl_n[p] = 0;
     }
     const uint32_t nbt = min(ld_relaxed(&hx->bt_n[p]), a.cap_bt);
-    update_tasks(a, sh, st, p, r, nbt, ex.wr, ex.nw);
+    // (the large vertices queued for iteration 2 fall far again: their windows
+    // start over the whole range, as in iteration 1)
+    update_tasks(a, sh, st, p, r, nbt, ex.wr, ex.nw, t == 1);
     if (!hx_barrier(a, sh)) return -1;
     ++r;
     const uint32_t nm = ld_relaxed(&hx->rm_n[p ^ 1u]), nl = ld_relaxed(&hx->rl_n[p ^ 1u]);
