@@ -56,6 +56,8 @@ struct ClSmem {
     uint32_t eall[kTailV];          // every vertex's estimate (a copy in each CTA)
     uint32_t cnt[kPer];
     uint32_t old[kPer];
+    uint32_t sdeg[kPer];            // induced degree and first quad of each slot (read once from L2)
+    uint32_t sfq[kPer];
     uint32_t front[2][kPer / 32];   // frontier bitmaps by iteration parity
     uint32_t work[kPer];            // phase A: slots of up to kWVals arcs; phase B: slots that dropped
     uint32_t big[kPer];             // slots the whole CTA handles
@@ -230,7 +232,7 @@ struct Tail {
             uint32_t s = kFull, d = 0;
             if (i < i1) {
                 s = sm.work[i];
-                d = degree(vertex(s));
+                d = sm.sdeg[s];
             }
             uint32_t tot;
             const uint32_t ex = warp_excl_scan(d, &tot);
@@ -248,7 +250,7 @@ struct Tail {
             const uint32_t qex = warp_excl_scan(lane < k1 ? (d + 3) / 4 : 0u, &qtot);
             qpref[lane] = qex;
             if (lane == 0) qpref[32] = qtot;
-            fq[lane] = lane < k1 ? first_quad(vertex(s)) : 0u;
+            fq[lane] = lane < k1 ? sm.sfq[s] : 0u;
             __syncwarp();
             gather_batch(qpref, fq, pref, k1, vals);
             __syncwarp();
@@ -276,7 +278,7 @@ struct Tail {
         if (threadIdx.x == 0) {
             uint32_t q = 0, v = 0;
             for (uint32_t i = 0; i < sm.nbig; ++i) {
-                const uint32_t d = degree(vertex(sm.big[i]));
+                const uint32_t d = sm.sdeg[sm.big[i]];
                 sm.bq[i] = q;
                 sm.bv[i] = v;
                 q += (d + 3) / 4;
@@ -329,7 +331,7 @@ struct Tail {
                     if (qf < qt) {
                         kk[u] = big_owner(qf + q0, i1, lo);
                         qi[u] = qf + q0 - sm.bq[kk[u]];
-                        x[u] = quad(first_quad(vertex(sm.big[kk[u]])) + qi[u]);
+                        x[u] = quad(sm.sfq[sm.big[kk[u]]] + qi[u]);
                     }
                 }
                 uint32_t val[16];
@@ -403,7 +405,7 @@ struct Tail {
                 if (qf < qt) {
                     kk[u] = big_owner(qf, nb, lo);
                     qi[u] = qf - sm.bq[kk[u]];
-                    x[u] = quad(first_quad(vertex(sm.big[kk[u]])) + qi[u]);
+                    x[u] = quad(sm.sfq[sm.big[kk[u]]] + qi[u]);
                 }
             }
             uint32_t id[16], xs[16];
@@ -439,7 +441,7 @@ struct Tail {
     // Phase A, CTA path: one slot of more than kWVals arcs, read whole.
     __device__ void recompute_cta(uint32_t s) {
         const unsigned tid = threadIdx.x;
-        const uint32_t v = vertex(s), q0 = first_quad(v), d = degree(v);
+        const uint32_t q0 = sm.sfq[s], d = sm.sdeg[s];
         const uint32_t e = sm.eall[vertex(s)];
         const uint32_t m = min(d, kCVals);
         gather(q0, m, sm.vals, tid, kClThreads);
@@ -481,9 +483,9 @@ struct Tail {
             uint32_t nq = 0;
             if (i < i1) {
                 const uint32_t s = sm.work[i], v = vertex(s);
-                const uint32_t d = degree(v);
+                const uint32_t d = sm.sdeg[s];
                 nq = (d + 3) / 4;
-                fq[lane] = first_quad(v);
+                fq[lane] = sm.sfq[s];
                 dd[lane] = d;
                 wn[lane] = sm.eall[v];
                 wo[lane] = sm.old[s];
@@ -569,7 +571,11 @@ __global__ void __launch_bounds__(kClThreads, 1) peel_hxtail_kernel(const __grid
     // vertices (a count below the estimate) in the first frontier
     for (uint32_t v = tid; v < kTailV; v += kClThreads)
         sm.eall[v] = v < n ? (ho ? __ldcg(a.tail_est + v) : T.degree(v)) : 0u;
-    for (uint32_t s = tid; s < kPer; s += kClThreads) sm.cnt[s] = ho && s < own ? __ldcg(a.tail_cnt + T.vertex(s)) : 0u;
+    for (uint32_t s = tid; s < kPer; s += kClThreads) {
+        sm.cnt[s] = ho && s < own ? __ldcg(a.tail_cnt + T.vertex(s)) : 0u;
+        sm.sdeg[s] = s < own ? T.degree(T.vertex(s)) : 0u;
+        sm.sfq[s] = s < own ? T.first_quad(T.vertex(s)) : 0u;
+    }
     for (uint32_t w = tid; w < 2 * (kPer / 32); w += kClThreads) (&sm.front[0][0])[w] = 0;
     if (tid == 0) {
         sm.flag[0] = sm.flag[1] = sm.flag[2] = 0;
@@ -592,7 +598,7 @@ __global__ void __launch_bounds__(kClThreads, 1) peel_hxtail_kernel(const __grid
         for (uint32_t s = tid; s < own; s += kClThreads) {
             const bool in = (t == 1 && !ho) || ((sm.front[p][s >> 5] >> (s & 31)) & 1u);
             if (!in) continue;
-            if (T.degree(T.vertex(s)) <= kWVals) sm.work[atomicAdd(&sm.nwork, 1u)] = s;
+            if (sm.sdeg[s] <= kWVals) sm.work[atomicAdd(&sm.nwork, 1u)] = s;
             else sm.big[atomicAdd(&sm.nbig, 1u)] = s;
         }
         __syncthreads();
@@ -606,7 +612,7 @@ __global__ void __launch_bounds__(kClThreads, 1) peel_hxtail_kernel(const __grid
         __syncthreads();
         for (uint32_t i = tid; i < min(sm.nchg, kPer); i += kClThreads) {
             const uint32_t s = sm.chg[i];
-            if (T.degree(T.vertex(s)) <= kWVals) sm.work[atomicAdd(&sm.nwork, 1u)] = s;
+            if (sm.sdeg[s] <= kWVals) sm.work[atomicAdd(&sm.nwork, 1u)] = s;
             else sm.big[atomicAdd(&sm.nbig, 1u)] = s;
         }
         __syncthreads();
