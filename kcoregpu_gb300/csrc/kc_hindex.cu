@@ -588,6 +588,11 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
         }
         nlo = sb;
         nhi = min(sb + (1u << shft) - 1u, hi);
+        // this pass over the adjacency rebuilt the list of the neighbours at or
+        // above lo - kListMargin: it holds every neighbour that can still reach
+        // the narrower window, so the next pass reads it when it is at most
+        // half the adjacency
+        if (mode == 0 && lo > 0 && 2u * __ldcg(a.alen + v) <= KC_LDG(a.off + v + 1) - KC_LDG(a.off + v)) nmode = 1;
     } else {   // h < lo (lo > 0 here: at lo = 0 bin 0 always qualifies)
         // the list still holds every neighbour down to its floor; below that
         // the adjacency is read
@@ -604,6 +609,7 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
     }
     uint32_t len = __ldcg(&sl->len);
     if (nmode == 0 && mode == 1) len = KC_LDG(a.off + v + 1) - KC_LDG(a.off + v);
+    if (nmode == 1 && mode == 0) len = __ldcg(a.alen + v);
     const uint32_t nch = (len + kHxChunk - 1) / kHxChunk;
     if (lane == 0) {
         sl->lo = nlo;
@@ -614,6 +620,7 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
         sl->nch = nch;
         sl->done = 0;
         if (nmode == 0) a.alen[v] = 0;   // the next pass rebuilds the list
+        if (nmode == 1 && mode == 0) a.alo[v] = lo > kListMargin ? lo - kListMargin : 0u;
         atomicAdd(&a.ctl->hx.passes, 1u);
     }
     queue_chunks(a, r, s, nch, lane, 32);
@@ -830,9 +837,15 @@ __device__ int hx_iteration(const HxArgs& a, HxShared& sh, Stager& st, uint32_t&
     HxCtl* hx = &a.ctl->hx;
     const unsigned lane = lane_id();
     const uint32_t p = t & 1u;
-    // ---- phase A: window passes; the first also takes the warp frontier
+    // ---- phase A: window passes; the first also takes the warp frontier.
+    // Every pass narrows each open window or ends it, so the passes are few;
+    // the cap only turns a broken invariant into an error instead of a loop.
     bool first = true;
-    for (;;) {
+    for (uint32_t npass = 0;; ++npass) {
+        if (npass > 4096) {   // (every CTA counts the same passes)
+            if (ex.lead) record_error(a.ctl, kErrOverflow, t);
+            return -1;
+        }
         const uint32_t ncl = min(ld_relaxed(&hx->cl_n[r % 3]), a.cap_cl);
         const uint32_t nrc = min(ld_relaxed(&hx->rc_n[r % 3]), a.cap_l);
         const uint32_t nrm = first ? min(ld_relaxed(&hx->rm_n[p]), a.V) : 0u;
