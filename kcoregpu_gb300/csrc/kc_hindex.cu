@@ -205,7 +205,7 @@ __device__ void open_window(const HxArgs& a, uint32_t q, uint32_t r, uint32_t v,
     sl.hi = hi;
     sl.mode = mode;
     sl.len = len;
-    if (mode == 0) a.alen[v] = 0;   // the pass rebuilds the list
+    if (mode == 0) a.alen[v] = lo > kListMargin ? 0u : kFull;   // the pass rebuilds the list (none from floor 0)
     sl.sh = bin_shift(lo, hi);
     sl.done = 0;
     sl.nch = (len + kHxChunk - 1) / kHxChunk;
@@ -561,10 +561,14 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
         const uint32_t Sb = __shfl_sync(kFull, S, bs);
         const uint32_t sb = lo + (bs << shft);
         if (shft == 0) {   // found: h = sb, counted Sb
-            // a pass over the adjacency leaves the list of neighbours >= lo
-            const uint32_t L = mode == 0 ? __ldcg(a.alen + v) : __ldcg(&sl->len);
+            // a pass over the adjacency leaves the list of neighbours >= lo -
+            // kListMargin (none from a window at or below kListMargin: the
+            // update then reads the adjacency)
+            const bool listed = mode == 1 || lo > kListMargin;
+            const uint32_t L = mode == 1 ? __ldcg(&sl->len)
+                                         : (listed ? __ldcg(a.alen + v) : KC_LDG(a.off + v + 1) - KC_LDG(a.off + v));
             if (lane == 0) {
-                if (mode == 0) a.alo[v] = lo > kListMargin ? lo - kListMargin : 0u;
+                if (mode == 0 && listed) a.alo[v] = lo - kListMargin;
                 a.cnt[v] = Sb;
                 if (sb < e) {
                     a.old[v] = e;
@@ -580,7 +584,7 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
                 if (lane == 0 && n) base = atomicAdd(&hx->bt_n[p], n);
                 base = __shfl_sync(kFull, base, 0);
                 for (uint32_t c = lane; c < n; c += 32) {
-                    if (base + c < a.cap_bt) a.bt[p][base + c] = ((unsigned long long)v << 32) | kListTask | c;
+                    if (base + c < a.cap_bt) a.bt[p][base + c] = ((unsigned long long)v << 32) | (listed ? kListTask : 0u) | c;
                     else record_error(a.ctl, kErrOverflow, 0);
                 }
             }
@@ -592,7 +596,8 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
         // above lo - kListMargin: it holds every neighbour that can still reach
         // the narrower window, so the next pass reads it when it is at most
         // half the adjacency
-        if (mode == 0 && lo > 0 && 2u * __ldcg(a.alen + v) <= KC_LDG(a.off + v + 1) - KC_LDG(a.off + v)) nmode = 1;
+        if (mode == 0 && lo > kListMargin && 2u * __ldcg(a.alen + v) <= KC_LDG(a.off + v + 1) - KC_LDG(a.off + v))
+            nmode = 1;
     } else {   // h < lo (lo > 0 here: at lo = 0 bin 0 always qualifies)
         // the list still holds every neighbour down to its floor; below that
         // the adjacency is read
@@ -619,7 +624,7 @@ __device__ void resolve_slot(const HxArgs& a, HxShared& sh, Stager& st, uint32_t
         sl->len = len;
         sl->nch = nch;
         sl->done = 0;
-        if (nmode == 0) a.alen[v] = 0;   // the next pass rebuilds the list
+        if (nmode == 0) a.alen[v] = nlo > kListMargin ? 0u : kFull;   // the next pass rebuilds the list
         if (nmode == 1 && mode == 0) a.alo[v] = lo > kListMargin ? lo - kListMargin : 0u;
         atomicAdd(&a.ctl->hx.passes, 1u);
     }
@@ -668,8 +673,9 @@ __device__ void chunk_task(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p
             bin[k] = x > hi ? 32u : (x >= lo ? (x - lo) >> shft : kNoBin);
         }
     }
-    if (mode == 0) {   // rebuild the active list: the neighbours at or above lo - kListMargin
-        const uint32_t lfl = lo > kListMargin ? lo - kListMargin : 0u;
+    if (mode == 0 && lo > kListMargin) {   // rebuild the active list: the neighbours at or above lo - kListMargin
+        // (a window from at most kListMargin keeps no list: it would hold every neighbour)
+        const uint32_t lfl = lo - kListMargin;
         unsigned keep[8];
         uint32_t nk = 0;
 #pragma unroll
