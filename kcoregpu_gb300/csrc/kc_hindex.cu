@@ -263,11 +263,26 @@ __device__ __forceinline__ uint32_t gallop_hindex(Ge ge, uint32_t fl, uint32_t e
     return lo;
 }
 
+// Largest h in [fl, e] with ge(h) >= h by bisection; kFull when ge(fl) < fl.
+// For iterations 1 and 2, where estimates fall far: about log2(e - fl) probes
+// against galloping's two per halving of the drop (1-2% off the benchmark
+// peels).
+template <class Ge>
+__device__ __forceinline__ uint32_t bisect_hindex(Ge ge, uint32_t fl, uint32_t e) {
+    if (ge(fl) < fl) return kFull;
+    uint32_t lo = fl, hi = e;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (ge(mid) >= mid) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Largest h in [fl, e] with at least h of the d values xs[0..d) >= h (d <=
 // kBatchVals, in shared memory), and the count at that h; kFull when fewer
 // than fl values are >= fl (the h-index lies below the floor).  One warp.
 __device__ __forceinline__ uint32_t warp_hindex(const uint32_t* xs, uint32_t d, uint32_t fl, uint32_t e,
-                                                uint32_t* count) {
+                                                uint32_t* count, bool far) {
     const unsigned lane = lane_id();
     constexpr int kPer = kBatchVals / 32;
     uint32_t x[kPer];
@@ -282,7 +297,7 @@ __device__ __forceinline__ uint32_t warp_hindex(const uint32_t* xs, uint32_t d, 
         for (int j = 0; j < kPer; ++j) c += (lane + 32u * j < d && x[j] >= h) ? 1u : 0u;
         return __reduce_add_sync(kFull, c);
     };
-    const uint32_t h = gallop_hindex(ge, fl, e);   // warp-uniform
+    const uint32_t h = far ? bisect_hindex(ge, fl, e) : gallop_hindex(ge, fl, e);   // warp-uniform
     if (h != kFull) *count = ge(h);
     return h;
 }
@@ -297,7 +312,7 @@ __device__ __forceinline__ uint32_t warp_hindex(const uint32_t* xs, uint32_t d, 
 // h-index from shared memory.  An h-index below a list's floor sends the
 // vertex to a window search over its adjacency in the next pass.
 __device__ void warp_batch(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p, uint32_t r, const uint32_t* list,
-                           uint32_t n, uint32_t wr, uint32_t nw) {
+                           uint32_t n, uint32_t wr, uint32_t nw, bool far) {
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     uint32_t* vals = sh.vals[wid];
     uint32_t* pref = sh.wbin[wid];   // 33 words: exclusive prefix of the degrees + total
@@ -382,7 +397,7 @@ __device__ void warp_batch(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p
                     for (uint32_t i2 = 0; i2 < d; ++i2) k += xs[i2] >= t ? 1u : 0u;
                     return k;
                 };
-                h = gallop_hindex(ge, fl, e);
+                h = far ? bisect_hindex(ge, fl, e) : gallop_hindex(ge, fl, e);
                 if (h != kFull) c = ge(h);
             }
             // larger entries: the warp, one after another
@@ -393,7 +408,7 @@ __device__ void warp_batch(const HxArgs& a, HxShared& sh, Stager& st, uint32_t p
                 const uint32_t dk = pref[k + 1] - pref[k];
                 const uint32_t ek = __shfl_sync(kFull, e, k), fk = __shfl_sync(kFull, fl, k);
                 uint32_t ck = 0;
-                const uint32_t hk = warp_hindex(vals + (pref[k] - base), dk, fk, ek, &ck);
+                const uint32_t hk = warp_hindex(vals + (pref[k] - base), dk, fk, ek, &ck, far);
                 if (lane == k) { h = hk; c = ck; }
             }
             // results: the lane of each entry writes it
@@ -443,7 +458,7 @@ __device__ __forceinline__ uint32_t cta_sum(uint32_t x, HxShared& sh) {
 // one pass, with CTA reductions.  An h-index below the list's floor sends the
 // CTA on to the adjacency, or, above kHxCtaVals arcs, to a window search in
 // the next pass.
-__device__ void cta_entry(const HxArgs& a, HxShared& sh, uint32_t p, uint32_t r, uint32_t ent) {
+__device__ void cta_entry(const HxArgs& a, HxShared& sh, uint32_t p, uint32_t r, uint32_t ent, bool far) {
     const unsigned tid = threadIdx.x, lane = lane_id();
     const uint32_t v = ent & ~kListFlag;
     if (v >= a.V) return;
@@ -481,7 +496,7 @@ __device__ void cta_entry(const HxArgs& a, HxShared& sh, uint32_t p, uint32_t r,
             for (int j = 0; j < kPer; ++j) c += (tid + kPeelThreads * j < len && x[j] >= h) ? 1u : 0u;
             return cta_sum(c, sh);
         };
-        const uint32_t h = gallop_hindex(ge, fl, e);   // CTA-uniform
+        const uint32_t h = far ? bisect_hindex(ge, fl, e) : gallop_hindex(ge, fl, e);   // CTA-uniform
         if (h == kFull) {   // below the list's floor
             list = false;
             __syncthreads();
@@ -868,7 +883,7 @@ __device__ int hx_iteration(const HxArgs& a, HxShared& sh, Stager& st, uint32_t&
             hx->rc_n[(r + 2) % 3] = 0;
         }
         if (nrc <= kCtaEntries * ex.ncta) {   // a CTA each, one after another
-            for (uint32_t i = ex.cta; i < nrc; i += ex.ncta) cta_entry(a, sh, p, r, __ldcg(a.rc[r % 3] + i));
+            for (uint32_t i = ex.cta; i < nrc; i += ex.ncta) cta_entry(a, sh, p, r, __ldcg(a.rc[r % 3] + i), t <= 2);
         } else {
             // too many for the CTAs: window searches spread over every warp,
             // from the next pass
@@ -880,7 +895,7 @@ __device__ int hx_iteration(const HxArgs& a, HxShared& sh, Stager& st, uint32_t&
                 }
             }
         }
-        if (nrm) warp_batch(a, sh, st, p, r, a.rm[p], nrm, ex.wr, ex.nw);
+        if (nrm) warp_batch(a, sh, st, p, r, a.rm[p], nrm, ex.wr, ex.nw, t <= 2);
         for (uint32_t i = ex.wr; i < ncl; i += ex.nw) chunk_task(a, sh, st, p, r, __ldcg(a.cl[r % 3] + i), t == 1);
         flush_bt(a, sh, st, p);
         if (!hx_barrier(a, sh)) return -1;
