@@ -48,6 +48,10 @@
 //     the bins, and either finds h (bins one wide) or narrows the window to
 //     the bin holding h (or the range below it) for another pass.  Every pass
 //     counts afresh, so the final h and its count come from one pass's reads.
+// Once the frontier is small, the last iterations go to a 16-CTA cluster
+// kernel (kc_hxtail.cu): the set of vertices at or above a floor T, handed
+// over only when every member has at least T neighbours in it (try_handoff
+// below), so that the vertices outside it are already final.
 // A graph that needs more than max_iters iterations (long paths converge one
 // hop per iteration) is left to the level peel: the kernel returns without
 // setting HxCtl::solved and the persistent and tail kernels run as usual.
