@@ -143,7 +143,8 @@ struct kc_graph {
     unsigned long long* d_hx_cl[3] = {nullptr, nullptr, nullptr};
     uint32_t* d_hx_rc[3] = {nullptr, nullptr, nullptr};
     unsigned long long* d_hx_bt[2] = {nullptr, nullptr};
-    uint32_t* d_hx_tail = nullptr;  // hand-off to the cluster: estimates and counts of S (kTailV each)
+    uint32_t* d_hx_tail = nullptr;  // hand-off to the cluster: ids, offsets (kTailV + 4), cursors,
+                                    // estimates and counts of S (kTailV each)
     uint32_t* d_hx_tnbr = nullptr;  // and its induced adjacency (spans as long as each member's source)
     uint32_t hx_tnbr_cap = 0;
     uint32_t hx_cap_v = 0, hx_cap_l = 0, hx_cap_cl = 0, hx_cap_bt = 0;
@@ -372,7 +373,7 @@ int reserve_hx(kc_graph* g) {
         set_error_msg("graph too large for the h-index peel");
         return KC_ERR_OVERFLOW;
     }
-    if (!g->d_hx_tail) KC_CUDA(cudaMalloc(&g->d_hx_tail, sizeof(uint32_t) * 2 * kTailV));
+    if (!g->d_hx_tail) KC_CUDA(cudaMalloc(&g->d_hx_tail, sizeof(uint32_t) * (5 * kTailV + 4)));
     {   // the hand-off's adjacency spans: up to every arc of the graph (at most 2^26), plus the quad padding
         const uint64_t cap = ((std::min<uint64_t>(std::max<uint64_t>(E, 1), 1ull << 26) + 3ull * kTailV + 16) + 3) & ~3ull;
         if (cap > g->hx_tnbr_cap) {
@@ -752,12 +753,13 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         h.after_peel = 0;
         // the hand-off to the cluster kernel (not after a level peel, whose
         // peeled vertices keep no counts)
-        const void* hof = (tail && !hindex_start()) ? hxhandoff_kernel(g->dev) : nullptr;
+        const void* hof = !hindex_start() ? hxhandoff_kernel(g->dev) : nullptr;
         h.handoff = hof ? 1u : 0u;
         h.lmap = g->d_hx_old;
-        h.tail_ids = g->d_tail_ids;
-        h.tail_off = g->d_tail_off;
-        h.tail_cur = g->d_tail_cur;
+        // (buffers of its own, not the level tail's: KC_TAIL_V does not touch it)
+        h.tail_ids = g->d_hx_tail + 2 * kTailV;
+        h.tail_cur = g->d_hx_tail + 3 * kTailV;
+        h.tail_off = g->d_hx_tail + 4 * kTailV;   // kTailV + 4 entries
         h.tail_nbr = g->d_hx_tnbr;
         h.tail_est = g->d_hx_tail;
         h.tail_cnt = g->d_hx_tail + kTailV;
@@ -787,6 +789,9 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
             ah.tail_est = h.tail_est;
             ah.tail_cnt = h.tail_cnt;
             ah.tail_nbr = h.tail_nbr;
+            ah.tail_ids = h.tail_ids;
+            ah.tail_off = h.tail_off;
+            ah.tail_cur = h.tail_cur;
             ah.tail_hx_iters = hxtail_max_iters();
             const int rc = launch_hxcluster(hof, &ah, g->stream);
             if (rc) return rc;

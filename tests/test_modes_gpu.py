@@ -9,8 +9,9 @@ KC_HX_ITERS=2 the level peel then starts over).  The h-index peel hands its
 last iterations to the cluster kernel by default: KC_HX_HANDOFF=0 keeps them
 in the grid, KC_HX_HO_FRONT=10^9 tries the hand-off from the third iteration
 on (large sets, failed certificates, later retries), KC_HX_HO_N=512 allows
-only small sets, and with KC_HX_TAIL_ITERS=2 the cluster gives up and the
-level peel runs from the start.  With KC_TAIL=hindex
+only small sets, with KC_HX_TAIL_ITERS=2 the cluster gives up and the level
+peel runs from the start, and KC_TAIL_V=0 (no level-peel tail buffers) leaves
+the hand-off, which has buffers of its own, in place.  With KC_TAIL=hindex
 the survivors handed to the tail go to the cluster h-index tail (16-CTA
 cluster, estimates in distributed shared memory); with KC_HX_TAIL_ITERS=2 it
 gives up and the level tail finishes them.
@@ -77,7 +78,7 @@ LEVEL_PEEL = [
 @pytest.mark.parametrize("env", [{"KC_ALGO": "peel", **e} for e in LEVEL_PEEL] +
                          [{"KC_ALGO": "hindex"}, {"KC_ALGO": "hindex", "KC_HX_ITERS": "3"},
                           {"KC_HX_START": "8"}, {"KC_HX_START": "8", "KC_HX_ITERS": "2"},
-                          {"KC_HX_HANDOFF": "0"}, {"KC_HX_HO_FRONT": "1000000000"},
+                          {"KC_HX_HANDOFF": "0"}, {"KC_HX_HO_FRONT": "1000000000"}, {"KC_TAIL_V": "0"},
                           {"KC_HX_HO_FRONT": "1000000000", "KC_HX_HO_N": "512"},
                           {"KC_HX_HO_FRONT": "1000000000", "KC_HX_TAIL_ITERS": "2"},
                           {"KC_ALGO": "peel", "KC_TAIL": "hindex"},
