@@ -143,8 +143,8 @@ struct kc_graph {
     unsigned long long* d_hx_cl[3] = {nullptr, nullptr, nullptr};
     uint32_t* d_hx_rc[3] = {nullptr, nullptr, nullptr};
     unsigned long long* d_hx_bt[2] = {nullptr, nullptr};
-    uint32_t* d_hx_tail = nullptr;  // hand-off to the cluster: ids, offsets (kTailV + 4), cursors,
-                                    // estimates and counts of S (kTailV each)
+    uint32_t* d_hx_tail = nullptr;  // hand-off to the cluster: ids, offsets (kHoV + 4), cursors,
+                                    // estimates and counts of S (kHoV each)
     uint32_t* d_hx_tnbr = nullptr;  // and its induced adjacency (spans as long as each member's source)
     uint32_t hx_tnbr_cap = 0;
     uint32_t hx_cap_v = 0, hx_cap_l = 0, hx_cap_cl = 0, hx_cap_bt = 0;
@@ -373,9 +373,9 @@ int reserve_hx(kc_graph* g) {
         set_error_msg("graph too large for the h-index peel");
         return KC_ERR_OVERFLOW;
     }
-    if (!g->d_hx_tail) KC_CUDA(cudaMalloc(&g->d_hx_tail, sizeof(uint32_t) * (5 * kTailV + 4)));
+    if (!g->d_hx_tail) KC_CUDA(cudaMalloc(&g->d_hx_tail, sizeof(uint32_t) * (5 * kHoV + 4)));
     {   // the hand-off's adjacency spans: up to every arc of the graph (at most 2^26), plus the quad padding
-        const uint64_t cap = ((std::min<uint64_t>(std::max<uint64_t>(E, 1), 1ull << 26) + 3ull * kTailV + 16) + 3) & ~3ull;
+        const uint64_t cap = ((std::min<uint64_t>(std::max<uint64_t>(E, 1), 1ull << 26) + 3ull * kHoV + 16) + 3) & ~3ull;
         if (cap > g->hx_tnbr_cap) {
             cudaFree(g->d_hx_tnbr);
             g->d_hx_tnbr = nullptr;
@@ -473,9 +473,9 @@ const void* hxhandoff_kernel(int dev) {
 
 // When the h-index peel tries the hand-off: once its frontier holds at most
 // KC_HX_HO_FRONT vertices (default 256), with S of at most KC_HX_HO_N
-// vertices (default and largest kTailV); read once per process.
+// vertices (default and largest kHoV); read once per process.
 void handoff_limits(uint32_t& front, uint32_t& nmax) {
-    static uint32_t f = 256, m = kTailV;
+    static uint32_t f = 256, m = kHoV;
     static std::once_flag once;
     std::call_once(once, [] {
         if (const char* e = std::getenv("KC_HX_HO_FRONT")) {
@@ -484,7 +484,7 @@ void handoff_limits(uint32_t& front, uint32_t& nmax) {
         }
         if (const char* e = std::getenv("KC_HX_HO_N")) {
             const long long x = std::atoll(e);
-            if (x >= 1 && x <= (long long)kTailV) m = (uint32_t)x;
+            if (x >= 1 && x <= (long long)kHoV) m = (uint32_t)x;
         }
     });
     front = f;
@@ -757,12 +757,12 @@ int graph_launch(kc_graph* g, bool with_order, bool with_trace = false) {
         h.handoff = hof ? 1u : 0u;
         h.lmap = g->d_hx_old;
         // (buffers of its own, not the level tail's: KC_TAIL_V does not touch it)
-        h.tail_ids = g->d_hx_tail + 2 * kTailV;
-        h.tail_cur = g->d_hx_tail + 3 * kTailV;
-        h.tail_off = g->d_hx_tail + 4 * kTailV;   // kTailV + 4 entries
+        h.tail_ids = g->d_hx_tail + 2 * kHoV;
+        h.tail_cur = g->d_hx_tail + 3 * kHoV;
+        h.tail_off = g->d_hx_tail + 4 * kHoV;   // kHoV + 4 entries
         h.tail_nbr = g->d_hx_tnbr;
         h.tail_est = g->d_hx_tail;
-        h.tail_cnt = g->d_hx_tail + kTailV;
+        h.tail_cnt = g->d_hx_tail + kHoV;
         h.tail_cap_arcs = g->hx_tnbr_cap;
         handoff_limits(h.ho_front, h.ho_max);
         if (const uint32_t n = hindex_start()) {

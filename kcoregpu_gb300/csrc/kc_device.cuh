@@ -278,6 +278,7 @@ struct PeelArgs {
 // Tail peel: one CTA of kTailThreads threads, states in shared memory.
 constexpr uint32_t kTailThreads = 1024;
 constexpr uint32_t kTailWarps = kTailThreads / 32;
+constexpr uint32_t kHoV = 24576;         // largest set the h-index peel hands to the cluster kernel
 constexpr uint32_t kTailV = 16384;        // largest tail (shared-memory states)
 constexpr uint32_t kTailHandoffV = 12288;  // default hand-off point (survivors); measured best of
                                            // 8,192 / 12,288 / 16,384 on the three single-graph workloads

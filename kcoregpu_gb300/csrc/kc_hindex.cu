@@ -944,7 +944,7 @@ __device__ int hx_iteration(const HxArgs& a, HxShared& sh, Stager& st, uint32_t&
 // stay valid (every neighbour they count has an estimate >= est >= T).  The
 // cluster continues the same iteration on the induced CSR of S from these
 // estimates and counts.  T is the smallest of T0/2, 5T0/8, ... T0 (T0 the
-// frontier's smallest estimate) that leaves at most kTailV vertices in S.
+// frontier's smallest estimate) that leaves at most kHoV vertices in S.
 
 constexpr uint32_t kHoMark = 0xFFFFFFFEu;   // lmap: a queued vertex (before the local ids are given)
 constexpr uint32_t kHoTask = 256;           // entries per chunk task of the hand-off
@@ -1056,7 +1056,7 @@ __device__ int try_handoff(const HxArgs& a, HxShared& sh, uint32_t t, uint32_t r
     }
     if (!hx_barrier(a, sh)) return -1;
     int pick = -1;
-    const uint32_t nmax = min(a.ho_max, kTailV);
+    const uint32_t nmax = min(a.ho_max, kHoV);
     for (int j = 0; j < kHoCand && pick < 0; ++j) {
         const uint32_t x = ld_relaxed(&hx->ho_cnt[P][j]);
         if (x > 0 && x <= nmax) pick = j;

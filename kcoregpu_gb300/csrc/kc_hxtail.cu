@@ -48,12 +48,12 @@ namespace {
 constexpr int kCl = 16;                     // CTAs of the cluster (non-portable size)
 constexpr int kClThreads = 512;
 constexpr int kClWarps = kClThreads / 32;
-constexpr uint32_t kPer = kTailV / kCl;     // vertices a CTA holds
+constexpr uint32_t kPer = kHoV / kCl;     // vertices a CTA holds
 constexpr uint32_t kWVals = 1024;           // values a warp gathers
 constexpr uint32_t kCVals = kClWarps * kWVals;   // values the CTA gathers
 
 struct ClSmem {
-    uint32_t eall[kTailV];          // every vertex's estimate (a copy in each CTA)
+    uint32_t eall[kHoV];          // every vertex's estimate (a copy in each CTA)
     uint32_t cnt[kPer];
     uint32_t old[kPer];
     uint32_t sdeg[kPer];            // induced degree and first quad of each slot (read once from L2)
@@ -562,14 +562,14 @@ __global__ void __launch_bounds__(kClThreads, 1) peel_hxtail_kernel(const __grid
     const bool ho = a.tail_est != nullptr;   // the launch after the h-index peel (hand-off mode)
     if (ctl->err != 0 || a.tail_hx_iters == 0 || (ho && ctl->hx.handoff == 0)) return;
     const uint32_t n = ho ? ctl->hx.ho_n : ctl->tail_n;
-    if (n == 0 || n > kTailV || (!ho && n > a.tail_cap_v)) return;
+    if (n == 0 || n > kHoV || (!ho && (n > a.tail_cap_v || n > kTailV))) return;
     Tail T{a, sm, cl, n, ho ? ctl->hx.ho_floor : ctl->tail_level, (uint32_t)cl.block_rank(), ctl->tail_arcs / 4u,
            reinterpret_cast<const uint4*>(a.tail_nbr)};
     const uint32_t own = n > T.rank ? (n - T.rank + kCl - 1) / kCl : 0u;
     // level tail: estimates from the induced degrees, every vertex in the first
     // frontier; hand-off: the h-index peel's estimates and counts, its queued
     // vertices (a count below the estimate) in the first frontier
-    for (uint32_t v = tid; v < kTailV; v += kClThreads)
+    for (uint32_t v = tid; v < kHoV; v += kClThreads)
         sm.eall[v] = v < n ? (ho ? __ldcg(a.tail_est + v) : T.degree(v)) : 0u;
     for (uint32_t s = tid; s < kPer; s += kClThreads) {
         sm.cnt[s] = ho && s < own ? __ldcg(a.tail_cnt + T.vertex(s)) : 0u;
