@@ -47,9 +47,9 @@ TIMING_NOTE = ("GPU arm: L2 flushed between timed steps (512 MiB write), inputs 
 # cluster kernel it hands its last iterations to, plus the level peel's
 # persistent and tail kernels (which return at once after it), and, for the
 # level peel method, its persistent and one-CTA tail kernels.
-NCU_TRAFFIC = {1: 30_896_384 + 710_400 + 7_269_376 + 66_048 + 29_184,
-               2: 59_834_112 + 8_267_776 + 273_664 + 65_536 + 29_440,
-               3: 84_490_240 + 24_905_216 + 1_509_632 + 65_792 + 29_184}
+NCU_TRAFFIC = {1: 30_764_800 + 712_192 + 7_332_352 + 65_792 + 29_184,
+               2: 63_110_144 + 10_822_656 + 839_424 + 66_816 + 29_184,
+               3: 84_662_016 + 25_049_088 + 1_640_704 + 65_536 + 28_928}
 NCU_TRAFFIC_LEVEL_PEEL = {1: 27_792_896 + 837_120 + 11_156_224, 2: 45_363_200 + 3_072_768 + 6_451_968 + 4_608,
                           3: 51_795_968 + 6_880_512 + 5_824_256}
 
