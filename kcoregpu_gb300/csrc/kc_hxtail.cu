@@ -13,12 +13,13 @@
 // peels in 50-148 levels and up to 637 dependent rounds converges in 34-60
 // iterations here.
 //
-// GB300 shape: the estimates, counts and frontier bitmaps live in the
-// distributed shared memory of a 16-CTA cluster (local id v in CTA v % kCl,
-// slot v / kCl), so a neighbour's estimate is a DSMEM load, a decrement a
-// DSMEM atomic, and the two barriers of an iteration are hardware cluster
-// barriers.  The induced adjacency (16-byte quads, pads 0xFFFFFFFF) is read
-// from L2.  Per iteration:
+// GB300 shape: one 16-CTA cluster.  Every CTA keeps a copy of all estimates
+// in its shared memory (up to kHoV = 24,576 vertices: 96 KB), so a
+// neighbour's estimate is a local load and a drop is broadcast by 16 DSMEM
+// stores; counts and frontier bitmaps live with their owner (local id v in
+// CTA v % kCl, slot v / kCl), so a decrement is a DSMEM atomic; the two
+// barriers of an iteration are hardware cluster barriers.  The induced
+// adjacency (16-byte quads, pads 0xFFFFFFFF) is read from L2.  Per iteration:
 //   phase A: each CTA recomputes its frontier vertices: up to kWVals arcs a
 //            warp (vertices batched so that their gathers overlap), larger
 //            ones the whole CTA, from values gathered into shared memory;
@@ -48,12 +49,12 @@ namespace {
 constexpr int kCl = 16;                     // CTAs of the cluster (non-portable size)
 constexpr int kClThreads = 512;
 constexpr int kClWarps = kClThreads / 32;
-constexpr uint32_t kPer = kHoV / kCl;     // vertices a CTA holds
+constexpr uint32_t kPer = kHoV / kCl;       // vertices a CTA owns
 constexpr uint32_t kWVals = 1024;           // values a warp gathers
 constexpr uint32_t kCVals = kClWarps * kWVals;   // values the CTA gathers
 
 struct ClSmem {
-    uint32_t eall[kHoV];          // every vertex's estimate (a copy in each CTA)
+    uint32_t eall[kHoV];            // every vertex's estimate (a copy in each CTA)
     uint32_t cnt[kPer];
     uint32_t old[kPer];
     uint32_t sdeg[kPer];            // induced degree and first quad of each slot (read once from L2)
