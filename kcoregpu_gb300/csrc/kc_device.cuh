@@ -121,8 +121,9 @@ struct alignas(128) HxCtl {
     unsigned int ho_m[2];        // members given local ids
     unsigned int ho_fail[2];     // a member has fewer than T neighbours in S, or a buffer is too small
     unsigned int ho_tasks[2];    // chunk tasks over the members' sources
-    unsigned int ho_arcs[2];     // induced-CSR entries reserved (each member: its source length, padded to quads)
-    unsigned int pad10[12];
+    unsigned long long ho_arcs[2];   // induced-CSR entries reserved (each member: its source length,
+                                     // padded to quads; 64 bits, so that no sum wraps)
+    unsigned int pad10[10];
 };
 
 struct alignas(128) PeelCtl {

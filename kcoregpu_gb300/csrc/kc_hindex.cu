@@ -1094,22 +1094,27 @@ __device__ int try_handoff(const HxArgs& a, HxShared& sh, uint32_t t, uint32_t r
                     }
                 }
             }
-            const uint32_t nch = (len + kHoTask - 1) / kHoTask, span = (len + 3u) & ~3u;
+            // (a span longer than the whole buffer fails below anyway; the clamp
+            // keeps a warp's sum of spans within 32 bits)
+            const uint32_t nch = (len + kHoTask - 1) / kHoTask;
+            const uint32_t span = min((len + 3u) & ~3u, a.tail_cap_arcs + 4u);
             uint32_t ntot, stot;
             const uint32_t cex = warp_excl_scan(nch, &ntot);
             const uint32_t sex = warp_excl_scan(span, &stot);
-            uint32_t b = 0, tb = 0, ab = 0;
+            uint32_t b = 0, tb = 0;
+            unsigned long long ab64 = 0;
             if (lane == 0) {
                 b = atomicAdd(&hx->ho_m[P], (uint32_t)__popc(m));
                 if (ntot) tb = atomicAdd(&hx->ho_tasks[P], ntot);
-                if (stot) ab = atomicAdd(&hx->ho_arcs[P], stot);
+                if (stot) ab64 = atomicAdd(&hx->ho_arcs[P], (unsigned long long)stot);
             }
             b = __shfl_sync(kFull, b, 0);
             tb = __shfl_sync(kFull, tb, 0) + cex;
-            ab = __shfl_sync(kFull, ab, 0) + sex;
+            ab64 = __shfl_sync(kFull, ab64, 0) + sex;
             if (in) {
                 const uint32_t lid = b + __popc(m & lanemask_lt());
-                if (lid < n && ab + span <= a.tail_cap_arcs && tb + nch <= a.cap_bt) {
+                if (lid < n && ab64 + span <= a.tail_cap_arcs && tb + nch <= a.cap_bt) {
+                    const uint32_t ab = (uint32_t)ab64;
                     a.lmap[v] = lid;
                     a.tail_ids[lid] = v;
                     a.tail_est[lid] = e[u];
@@ -1164,7 +1169,7 @@ __device__ int try_handoff(const HxArgs& a, HxShared& sh, uint32_t t, uint32_t r
         if (end - o < T) atomicOr(&hx->ho_fail[P], 1u);
         for (uint32_t q = end; q < ((end + 3u) & ~3u) && q < a.tail_cap_arcs; ++q) a.tail_nbr[q] = kFull;
     }
-    if (ex.lead) a.ctl->tail_arcs = min(ld_relaxed(&hx->ho_arcs[P]), a.tail_cap_arcs);
+    if (ex.lead) a.ctl->tail_arcs = (uint32_t)min(__ldcg(&hx->ho_arcs[P]), (unsigned long long)a.tail_cap_arcs);
     if (!hx_barrier(a, sh)) return -1;
     if (ld_relaxed(&hx->ho_fail[P])) return 2;
     if (ex.lead) {
